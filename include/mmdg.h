@@ -1,0 +1,133 @@
+/*
+ * mmdg.h -- C ABI of the GB300-native McMurchie-Davidson two-electron hot path.
+ *
+ * Plain C: device pointers, host arrays, sizes and an opaque context.  No torch or
+ * C++ types cross this boundary; a ctypes/cffi/cgo caller binds it directly.
+ * Every entry point returns 0 on success or a negative MMDG_E* code; the text of
+ * the last failure on the calling thread is available from mmdg_last_error().
+ *
+ * Each entry point replaces one interface of jjgoings/McMurchie-Davidson (cited
+ * as file:line within that project):
+ *
+ *   mmdg_set_basis    <- Basis construction (cython/basis.pxi:46-120) and the
+ *                        list-of-Basis argument of doERIs/formPT (cython/twoe.pyx:12,
+ *                        cython/fock.pyx:13): the function list is grouped into
+ *                        shells and turned into primitive-pair data on the GPU.
+ *   mmdg_get_screen   <- the Schwarz dict of Molecule.build(direct=True)
+ *                        (mmd/molecule.py:95-99): screen[p(p+1)/2+q] = (pq|pq).
+ *   mmdg_eri_tensor   <- doERIs (cython/twoe.pyx:12-31) / Molecule.two_electron_integrals
+ *                        (mmd/molecule.py:288-293): the full N^4 ERI tensor.
+ *   mmdg_fock         <- formPT (cython/fock.pyx:13-87): unsymmetrised two-electron
+ *                        Fock update G(P - P_old) with Schwarz x density screening.
+ *   mmdg_set_screen   <- the `screen` argument of formPT (cython/fock.pyx:13,46-47).
+ *   mmdg_jk_dense     <- the conventional J/K einsums of buildFock (mmd/scf.py:97-98).
+ *   mmdg_fock_update  <- G = (G + G^T)/2, F = F_old + G of buildFock (mmd/scf.py:91-94).
+ *   mmdg_one_electron <- S, T, V, Mu of cython/onee.pyx:14-192 as assembled by
+ *                        Molecule.one_electron_integrals (mmd/molecule.py:235-276).
+ *   mmdg_boys         <- boys / the _boys test hook (cython/util.pxi:54-55,
+ *                        cython/onee.pyx:195-196).
+ */
+#ifndef MMDG_H
+#define MMDG_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMDG_OK 0
+#define MMDG_E_ARG (-1)      /* invalid argument (null pointer, bad size, bad shell data) */
+#define MMDG_E_LMAX (-2)     /* angular momentum above the supported maximum (d, l = 2) */
+#define MMDG_E_CUDA (-3)     /* a CUDA runtime call failed */
+#define MMDG_E_STATE (-4)    /* call order: no basis set yet, or wrong molecule layout */
+#define MMDG_E_NOMEM (-5)    /* device allocation failed */
+
+#define MMDG_LMAX 2          /* highest shell angular momentum (Cartesian d) */
+#define MMDG_MAX_COMP 6      /* Cartesian components of a d shell */
+#define MMDG_NCLASS 21       /* angular classes (la lb|lc ld), la>=lb, lc>=ld, (la,lb)>=(lc,ld) */
+
+typedef struct mmdg_context mmdg_context;
+
+/* Thread-local text of the last failure ("" if none). */
+const char* mmdg_last_error(void);
+
+/* Create a context on CUDA device `device` (allocates its Boys tables). */
+int mmdg_create(mmdg_context** out, int device);
+int mmdg_destroy(mmdg_context* ctx);
+
+/*
+ * Set the basis of one or more molecules (host arrays) and build, on the device,
+ * the primitive-pair data and the Schwarz table.  Synchronous.
+ *
+ *   nmol               number of molecules (1 for a single system)
+ *   mol_nfunc[nmol]    basis functions N_m of each molecule
+ *   nshell             number of shells over all molecules
+ *   shell_mol[s]       molecule of shell s (shells of a molecule are contiguous)
+ *   shell_L[s]         angular momentum 0..MMDG_LMAX
+ *   shell_nprim[s]     primitives (>= 1)
+ *   shell_center[3s]   centre, bohr
+ *   prim_exp[], prim_coef[]  primitives of all shells, shell after shell; prim_coef is
+ *                      the contraction coefficient times the contracted normalisation
+ *                      times the primitive normalisation of an x^L Cartesian
+ *                      component (the per-component factor 1/sqrt((2l-1)!!(2m-1)!!(2n-1)!!)
+ *                      is applied inside)
+ *   shell_func[6s+c]   molecule-local function index of Cartesian component c
+ *                      (order xx,xy,xz,yy,yz,zz for d; x,y,z for p), or -1 if that
+ *                      component is not part of the basis
+ */
+int mmdg_set_basis(mmdg_context* ctx, int nmol, const int* mol_nfunc, int nshell, const int* shell_mol,
+                   const int* shell_L, const int* shell_nprim, const double* shell_center, const double* prim_exp,
+                   const double* prim_coef, const int* shell_func);
+
+/* Copy the Schwarz table (pq|pq), packed per molecule as N_m(N_m+1)/2 entries
+ * in row order p(p+1)/2+q, to the host array `screen` of length n. */
+int mmdg_get_screen(mmdg_context* ctx, double* screen, long long n);
+
+/* Replace the Schwarz table by the caller's values (same layout as mmdg_get_screen),
+ * as formPT takes its `screen` dict from the caller (cython/fock.pyx:13,46-47);
+ * the per-shell-pair bounds are recomputed from it. */
+int mmdg_set_screen(mmdg_context* ctx, const double* screen, long long n);
+
+/* Full ERI tensor of molecule 0: out is a device array of N^4 doubles (C order). */
+int mmdg_eri_tensor(mmdg_context* ctx, double* out, void* stream);
+
+/*
+ * Direct two-electron Fock update (formPT semantics).
+ *   dP        device, packed per-molecule N_m x N_m blocks: P - P_old (real)
+ *   G         device, same layout; overwritten with the unsymmetrised update
+ *   tol       screening threshold (acc2e of RHF; reference default 1e-12)
+ *   fp32_below  shell quartets whose Schwarz bound Q_ab*Q_cd is below this value are
+ *             evaluated in FP32 (0 = all FP64, the plain method)
+ *   counts    optional host array of 3*MMDG_NCLASS unsigned long long: per class the
+ *             shell quartets, primitive quartets and function quartets computed
+ *             (filled after a stream synchronisation; pass NULL to stay asynchronous)
+ */
+int mmdg_fock(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below,
+              unsigned long long* counts, void* stream);
+
+/* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
+int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
+
+/* Symmetrised incremental Fock update of packed per-molecule blocks:
+ * F_out = F_in + (G + G^T)/2   (mmd/scf.py:91-94). Device arrays; F_out may alias F_in. */
+int mmdg_fock_update(mmdg_context* ctx, const double* G, const double* F_in, double* F_out, void* stream);
+
+/* Conventional Coulomb and exchange matrices from a dense ERI tensor
+ * (mmd/scf.py:97-98):  J_pq = sum_rs (pq|rs) P_sr,  K_pq = sum_rs (ps|qr) P_sr.
+ * All device arrays: T is N^4, P, J, K are N x N. */
+int mmdg_jk_dense(mmdg_context* ctx, long long N, const double* T, const double* P, double* J, double* K,
+                  void* stream);
+
+/* One-electron integrals S, T, V and the dipole integrals M (3 blocks) of every
+ * molecule, packed like mmdg_fock's G (cython/onee.pyx:14-192, assembled as
+ * Molecule.one_electron_integrals, mmd/molecule.py:235-276).  Atoms sorted by
+ * molecule: atom_mol[natom], atom_xyz[3*natom] (bohr), atom_Z[natom]; origin[3*nmol]
+ * is the dipole gauge origin of each molecule.  Outputs are device arrays of
+ * sum N_m^2 doubles (M: 3 x that). */
+int mmdg_one_electron(mmdg_context* ctx, int natom, const int* atom_mol, const double* atom_xyz,
+                      const double* atom_Z, const double* origin, double* S, double* T, double* V, double* M,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MMDG_H */

@@ -1,0 +1,1038 @@
+// capi.cu -- C ABI (include/mmdg.h): context, basis set-up, primitive pairs,
+// Schwarz table, Fock builds, ERI tensor, Boys evaluation.
+//
+// Host-side bookkeeping (shell pairs, class lists, offsets) is integer work done
+// once per basis; every floating-point quantity of the hot path is computed on
+// the GPU by the kernels below and in md_inst*.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/mmdg.h"
+#include "md_dispatch.cuh"
+
+using namespace mmdg;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+#define CUDA_TRY(x)                                                                                  \
+  do {                                                                                               \
+    cudaError_t e_ = (x);                                                                            \
+    if (e_ != cudaSuccess) return fail(MMDG_E_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+extern "C" const char* mmdg_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------------ device buffers
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+  }
+  cudaError_t upload(const std::vector<T>& v) {
+    cudaError_t e = alloc(v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  }
+};
+
+// ------------------------------------------------------------------ Boys table
+// F_m(T_k), T_k = k/16, by the Kummer-transformed series
+//   F_m(T) = exp(-T) / (2m+1) * sum_i T^i / ((m+3/2)(m+5/2)...(m+1/2+i))
+// at the highest order m = 14, then downward recursion
+//   F_{m-1} = (2T F_m + exp(-T)) / (2m-1),
+// all in double-double arithmetic (error-free transformations with fma), so the
+// table is correctly rounded to double and identical on every host.
+namespace {
+struct dd {
+  double hi, lo;
+};
+inline dd two_sum(double a, double b) {
+  double s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+inline dd quick_two_sum(double a, double b) {
+  double s = a + b;
+  return {s, b - (s - a)};
+}
+inline dd dd_add(dd a, dd b) {
+  dd s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+inline dd dd_mul(dd a, dd b) {
+  double p = a.hi * b.hi;
+  double e = std::fma(a.hi, b.hi, -p);
+  e += a.hi * b.lo + a.lo * b.hi;
+  return quick_two_sum(p, e);
+}
+inline dd dd_mul_d(dd a, double b) {
+  double p = a.hi * b;
+  double e = std::fma(a.hi, b, -p);
+  e += a.lo * b;
+  return quick_two_sum(p, e);
+}
+inline dd dd_div_d(dd a, double b) {
+  double q1 = a.hi / b;
+  dd r = dd_add(a, dd_mul_d({q1, 0.0}, -b));
+  double q2 = r.hi / b;
+  r = dd_add(r, dd_mul_d({q2, 0.0}, -b));
+  double q3 = r.hi / b;
+  dd q = quick_two_sum(q1, q2);
+  return dd_add(q, {q3, 0.0});
+}
+// exp(-x) for x = 1/16 by its Taylor series in double-double
+dd dd_exp_m16() {
+  dd term{1.0, 0.0}, sum{1.0, 0.0};
+  for (int n = 1; n < 40; ++n) {
+    term = dd_div_d(term, -16.0 * n);
+    sum = dd_add(sum, term);
+  }
+  return sum;
+}
+}  // namespace
+
+static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) {
+  t64.assign(kBoysNGrid * kBoysNCol, 0.0);
+  t32.assign(kBoysNGrid * kBoysNCol, 0.0f);
+  const dd e16 = dd_exp_m16();
+  dd eT{1.0, 0.0};
+  const int mtop = kBoysNCol - 2;  // 14
+  for (int k = 0; k < kBoysNGrid; ++k) {
+    if (k > 0) eT = dd_mul(eT, e16);
+    const double T = k / 16.0;
+    // series at m = mtop
+    dd term{1.0, 0.0}, sum{1.0, 0.0};
+    const double b = mtop + 1.5;
+    for (int i = 0; i < 2000; ++i) {
+      term = dd_div_d(dd_mul_d(term, T), b + i);
+      sum = dd_add(sum, term);
+      if (term.hi < sum.hi * 1e-34) break;
+    }
+    dd F[kBoysNCol];
+    F[mtop] = dd_div_d(dd_mul(eT, sum), 2.0 * mtop + 1.0);
+    for (int m = mtop; m > 0; --m) F[m - 1] = dd_div_d(dd_add(dd_mul_d(F[m], 2.0 * T), eT), 2.0 * m - 1.0);
+    for (int m = 0; m <= mtop; ++m) t64[k * kBoysNCol + m] = F[m].hi + F[m].lo;
+    t64[k * kBoysNCol + kBoysNCol - 1] = eT.hi + eT.lo;
+  }
+  for (size_t i = 0; i < t64.size(); ++i) t32[i] = float(t64[i]);
+}
+
+// ------------------------------------------------------------------ context
+static int nnz_pair(int la, int lb) {
+  int n = 0;
+  for (int xa = la; xa >= 0; --xa)
+    for (int ya = la - xa; ya >= 0; --ya) {
+      int za = la - xa - ya;
+      for (int xb = lb; xb >= 0; --xb)
+        for (int yb = lb - xb; yb >= 0; --yb) {
+          int zb = lb - xb - yb;
+          n += (xa + xb + 1) * (ya + yb + 1) * (za + zb + 1);
+        }
+    }
+  return n;
+}
+static int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
+static const int kNumPairClasses = (MMDG_LMAX + 1) * (MMDG_LMAX + 2) / 2;
+
+struct mmdg_context {
+  int device = 0;
+  bool have_basis = false;
+  DevBuf<double> boys64;
+  DevBuf<float> boys32;
+  // basis
+  int nmol = 0, nshell = 0;
+  std::vector<int> mol_n, mol_ns;
+  std::vector<long long> mol_base, mol_sbase, mol_tbase;
+  long long ntot_nn = 0, ntot_ss = 0, ntot_tri = 0;
+  DevBuf<double> d_center, d_exp, d_coef;
+  DevBuf<int> d_L, d_nprim, d_poff, d_func, d_shmol, d_shlocal;
+  DevBuf<long long> d_mol_base, d_mol_sbase, d_mol_tbase;
+  DevBuf<int> d_mol_n, d_mol_ns;
+  // pairs
+  int npair = 0;
+  long long nprimpair = 0, nE = 0;
+  std::vector<int> pa, pb, pcls, pr_begin, pr_count;
+  std::vector<long long> e_off;
+  DevBuf<int> d_pa, d_pb, d_prb, d_prc;
+  DevBuf<long long> d_eoff;
+  DevBuf<double4_32a> d_pP;
+  DevBuf<float4> d_pPf;
+  DevBuf<double> d_E64;
+  DevBuf<float> d_E32;
+  DevBuf<float> d_Q;
+  // class lists (sorted by primitive count, then Q descending)
+  std::vector<int> cls_count;
+  DevBuf<int> d_cls[kNumPairClasses];
+  // screening / Fock scratch
+  DevBuf<double> d_screen, d_sq;
+  DevBuf<float> d_sqf, d_dPf, d_Dsh;
+  DevBuf<unsigned long long> d_counters;
+  Geometry geom() const {
+    Geometry g;
+    g.pP = d_pP.p;
+    g.pPf = d_pPf.p;
+    g.E64 = d_E64.p;
+    g.E32 = d_E32.p;
+    g.pr_begin = d_prb.p;
+    g.pr_count = d_prc.p;
+    g.e_off = d_eoff.p;
+    g.pa = d_pa.p;
+    g.pb = d_pb.p;
+    g.Q = d_Q.p;
+    g.func = d_func.p;
+    g.sh_mol = d_shmol.p;
+    g.sh_local = d_shlocal.p;
+    g.mol_base = d_mol_base.p;
+    g.mol_n = d_mol_n.p;
+    g.mol_sbase = d_mol_sbase.p;
+    g.mol_ns = d_mol_ns.p;
+    g.mol_tbase = d_mol_tbase.p;
+    g.boys64 = boys64.p;
+    g.boys32 = boys32.p;
+    return g;
+  }
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+extern "C" int mmdg_create(mmdg_context** out, int device) {
+  if (!out) return fail(MMDG_E_ARG, "mmdg_create: null output pointer");
+  int ndev = 0;
+  CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(MMDG_E_ARG, "mmdg_create: no such CUDA device");
+  DeviceGuard dg(device);
+  mmdg_context* h = new mmdg_context();
+  h->device = device;
+  std::vector<double> t64;
+  std::vector<float> t32;
+  build_boys_table(t64, t32);
+  if (h->boys64.upload(t64) != cudaSuccess || h->boys32.upload(t32) != cudaSuccess) {
+    delete h;
+    return fail(MMDG_E_NOMEM, "mmdg_create: cannot allocate the Boys tables");
+  }
+  for (int g = 0; g < kNumGroups; ++g) {
+    cudaError_t e = kGroupInit[g]();
+    if (e != cudaSuccess) {
+      delete h;
+      return fail(MMDG_E_CUDA, std::string("mmdg_create: kernel set-up: ") + cudaGetErrorString(e));
+    }
+  }
+  *out = h;
+  return MMDG_OK;
+}
+
+extern "C" int mmdg_destroy(mmdg_context* h) {
+  if (!h) return MMDG_OK;
+  DeviceGuard dg(h->device);
+  delete h;
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ pair kernel
+// One thread per shell pair: primitive-pair data (p, P) and the E' tables
+//   E'[fa fb][t u v] = c_a c_b exp(-mu |AB|^2) / p * n(fa) n(fb) * Ex_t Ey_u Ez_v
+// with the 1D Hermite expansion coefficients of cython/util.pxi:13-28 built by
+// the same recursion (base E_0^{00} = 1; the Gaussian factor is K_ab):
+//   E^{i+1,j}_t = E^{ij}_{t-1}/(2p) + X_PA E^{ij}_t + (t+1) E^{ij}_{t+1}
+//   E^{i,j+1}_t = E^{ij}_{t-1}/(2p) + X_PB E^{ij}_t + (t+1) E^{ij}_{t+1}
+// n(lmn) = 1/sqrt((2l-1)!!(2m-1)!!(2n-1)!!) is the component part of the
+// primitive normalisation of cython/basis.pxi:101-105.
+__device__ __forceinline__ double comp_norm(int l) { return l >= 2 ? 0.57735026918962576 : 1.0; }
+
+struct PairBuildArgs {
+  int npair;
+  const int *pa, *pb, *prb;
+  const long long* eoff;
+  const int *L, *nprim, *poff;
+  const double *center, *exps, *coefs;
+  double4_32a* pP;
+  float4* pPf;
+  double* E64;
+  float* E32;
+};
+
+__global__ void k_build_pairs(PairBuildArgs a) {
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= a.npair) return;
+  const int sa = a.pa[pr], sb = a.pb[pr];
+  const int la = a.L[sa], lb = a.L[sb];
+  const int Ka = a.nprim[sa], Kb = a.nprim[sb];
+  const double Ax = a.center[3 * sa], Ay = a.center[3 * sa + 1], Az = a.center[3 * sa + 2];
+  const double Bx = a.center[3 * sb], By = a.center[3 * sb + 1], Bz = a.center[3 * sb + 2];
+  const double ABx = Ax - Bx, ABy = Ay - By, ABz = Az - Bz;
+  const double AB2 = ABx * ABx + ABy * ABy + ABz * ABz;
+  int nnz = 0;
+  for (int xa = la; xa >= 0; --xa)
+    for (int ya = la - xa; ya >= 0; --ya)
+      for (int xb = lb; xb >= 0; --xb)
+        for (int yb = lb - xb; yb >= 0; --yb)
+          nnz += (xa + xb + 1) * (ya + yb + 1) * ((la - xa - ya) + (lb - xb - yb) + 1);
+  const double AB[3] = {ABx, ABy, ABz};
+  for (int ka = 0; ka < Ka; ++ka)
+    for (int kb = 0; kb < Kb; ++kb) {
+      const int k = ka * Kb + kb;
+      const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+      const double p = ea + eb, ip = 1.0 / p, mu = ea * eb * ip;
+      const double Px = (ea * Ax + eb * Bx) * ip, Py = (ea * Ay + eb * By) * ip, Pz = (ea * Az + eb * Bz) * ip;
+      const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * ip;
+      const long long pp = a.prb[pr] + k;
+      a.pP[pp] = make_double4_32a(p, Px, Py, Pz);
+      a.pPf[pp] = make_float4(float(p), float(Px), float(Py), float(Pz));
+      // 1D tables E[d][i][j][t], i<=2, j<=2, t<=4
+      double E[3][3][3][5];
+      const double i2p = 0.5 * ip;
+      for (int d = 0; d < 3; ++d) {
+        const double XPA = -(eb * ip) * AB[d], XPB = (ea * ip) * AB[d];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j)
+            for (int t = 0; t < 5; ++t) E[d][i][j][t] = 0.0;
+        E[d][0][0][0] = 1.0;
+        for (int i = 0; i < la; ++i)
+          for (int t = 0; t <= i + 1; ++t) {
+            double v = XPA * E[d][i][0][t];
+            if (t > 0) v += i2p * E[d][i][0][t - 1];
+            if (t + 1 <= i) v += (t + 1) * E[d][i][0][t + 1];
+            E[d][i + 1][0][t] = v;
+          }
+        for (int j = 0; j < lb; ++j)
+          for (int i = 0; i <= la; ++i)
+            for (int t = 0; t <= i + j + 1; ++t) {
+              double v = XPB * E[d][i][j][t];
+              if (t > 0) v += i2p * E[d][i][j][t - 1];
+              if (t + 1 <= i + j) v += (t + 1) * E[d][i][j][t + 1];
+              E[d][i][j + 1][t] = v;
+            }
+      }
+      long long o = a.eoff[pr] + (long long)k * nnz;
+      for (int xa = la; xa >= 0; --xa)
+        for (int ya = la - xa; ya >= 0; --ya) {
+          const int za = la - xa - ya;
+          const double na = comp_norm(xa) * comp_norm(ya) * comp_norm(za);
+          for (int xb = lb; xb >= 0; --xb)
+            for (int yb = lb - xb; yb >= 0; --yb) {
+              const int zb = lb - xb - yb;
+              const double c = K * na * comp_norm(xb) * comp_norm(yb) * comp_norm(zb);
+              for (int t = 0; t <= xa + xb; ++t)
+                for (int u = 0; u <= ya + yb; ++u)
+                  for (int v = 0; v <= za + zb; ++v) {
+                    const double e = c * E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][v];
+                    a.E64[o] = e;
+                    a.E32[o] = float(e);
+                    ++o;
+                  }
+            }
+        }
+    }
+}
+
+// sqrt of the screen table (FP64 and FP32 copies)
+__global__ void k_sqrt_screen(const double* screen, double* sq, float* sqf, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = sqrt(fmax(screen[i], 0.0));
+  sq[i] = s;
+  sqf[i] = float(s);
+}
+
+// ------------------------------------------------------------------ set basis
+extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, int nshell, const int* shell_mol,
+                              const int* shell_L, const int* shell_nprim, const double* shell_center,
+                              const double* prim_exp, const double* prim_coef, const int* shell_func) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_basis: null context");
+  if (nmol < 1 || nshell < 1 || !mol_nfunc || !shell_mol || !shell_L || !shell_nprim || !shell_center ||
+      !prim_exp || !prim_coef || !shell_func)
+    return fail(MMDG_E_ARG, "mmdg_set_basis: empty basis or null array");
+  DeviceGuard dgd(h->device);
+  h->have_basis = false;
+  // ---- molecules and shells
+  h->nmol = nmol;
+  h->nshell = nshell;
+  h->mol_n.assign(mol_nfunc, mol_nfunc + nmol);
+  h->mol_ns.assign(nmol, 0);
+  std::vector<int> shlocal(nshell), poff(nshell);
+  int total_prim = 0;
+  for (int s = 0; s < nshell; ++s) {
+    const int m = shell_mol[s];
+    if (m < 0 || m >= nmol) return fail(MMDG_E_ARG, "mmdg_set_basis: shell_mol out of range");
+    if (s > 0 && m < shell_mol[s - 1]) return fail(MMDG_E_ARG, "mmdg_set_basis: shells of a molecule must be contiguous");
+    if (shell_L[s] < 0) return fail(MMDG_E_ARG, "mmdg_set_basis: negative angular momentum");
+    if (shell_L[s] > MMDG_LMAX)
+      return fail(MMDG_E_LMAX, "mmdg_set_basis: shell angular momentum " + std::to_string(shell_L[s]) +
+                                   " above the supported maximum " + std::to_string(MMDG_LMAX));
+    if (shell_nprim[s] < 1) return fail(MMDG_E_ARG, "mmdg_set_basis: shell without primitives");
+    shlocal[s] = h->mol_ns[m]++;
+    poff[s] = total_prim;
+    total_prim += shell_nprim[s];
+    const int nc = (shell_L[s] + 1) * (shell_L[s] + 2) / 2;
+    for (int c = 0; c < MMDG_MAX_COMP; ++c) {
+      const int f = shell_func[s * MMDG_MAX_COMP + c];
+      if (c >= nc && f >= 0) return fail(MMDG_E_ARG, "mmdg_set_basis: function index on a missing component");
+      if (f >= h->mol_n[m]) return fail(MMDG_E_ARG, "mmdg_set_basis: function index out of range");
+    }
+  }
+  for (int p = 0; p < total_prim; ++p)
+    if (!(prim_exp[p] > 0.0) || !std::isfinite(prim_exp[p]) || !std::isfinite(prim_coef[p]))
+      return fail(MMDG_E_ARG, "mmdg_set_basis: exponents must be positive and finite");
+  for (int s = 0; s < 3 * nshell; ++s)
+    if (!std::isfinite(shell_center[s])) return fail(MMDG_E_ARG, "mmdg_set_basis: non-finite centre");
+  h->mol_base.assign(nmol, 0);
+  h->mol_sbase.assign(nmol, 0);
+  h->mol_tbase.assign(nmol, 0);
+  long long nn = 0, ss = 0, tt = 0;
+  for (int m = 0; m < nmol; ++m) {
+    h->mol_base[m] = nn;
+    h->mol_sbase[m] = ss;
+    h->mol_tbase[m] = tt;
+    nn += (long long)h->mol_n[m] * h->mol_n[m];
+    ss += (long long)h->mol_ns[m] * h->mol_ns[m];
+    tt += (long long)h->mol_n[m] * (h->mol_n[m] + 1) / 2;
+  }
+  h->ntot_nn = nn;
+  h->ntot_ss = ss;
+  h->ntot_tri = tt;
+  // ---- shell pairs within each molecule (a has the higher L)
+  h->pa.clear();
+  h->pb.clear();
+  h->pcls.clear();
+  h->pr_begin.clear();
+  h->pr_count.clear();
+  h->e_off.clear();
+  long long npp = 0, ne = 0;
+  for (int s1 = 0; s1 < nshell; ++s1)
+    for (int s2 = s1; s2 >= 0 && shell_mol[s2] == shell_mol[s1]; --s2) {
+      int a = s1, b = s2;
+      if (shell_L[a] < shell_L[b]) std::swap(a, b);
+      const int cls = pair_class(shell_L[a], shell_L[b]);
+      const int np = shell_nprim[a] * shell_nprim[b];
+      h->pa.push_back(a);
+      h->pb.push_back(b);
+      h->pcls.push_back(cls);
+      h->pr_begin.push_back((int)npp);
+      h->pr_count.push_back(np);
+      h->e_off.push_back(ne);
+      npp += np;
+      ne += (long long)np * nnz_pair(shell_L[a], shell_L[b]);
+    }
+  if (npp > 0x7fffffffLL) return fail(MMDG_E_ARG, "mmdg_set_basis: too many primitive pairs");
+  h->npair = (int)h->pa.size();
+  h->nprimpair = npp;
+  h->nE = ne;
+  // ---- upload
+  std::vector<int> vL(shell_L, shell_L + nshell), vK(shell_nprim, shell_nprim + nshell);
+  std::vector<int> vfunc(shell_func, shell_func + (size_t)nshell * MMDG_MAX_COMP), vmol(shell_mol, shell_mol + nshell);
+  std::vector<double> vc(shell_center, shell_center + 3 * (size_t)nshell);
+  std::vector<double> ve(prim_exp, prim_exp + total_prim), vco(prim_coef, prim_coef + total_prim);
+  bool ok = h->d_L.upload(vL) == cudaSuccess && h->d_nprim.upload(vK) == cudaSuccess &&
+            h->d_poff.upload(poff) == cudaSuccess && h->d_func.upload(vfunc) == cudaSuccess &&
+            h->d_shmol.upload(vmol) == cudaSuccess && h->d_shlocal.upload(shlocal) == cudaSuccess &&
+            h->d_center.upload(vc) == cudaSuccess && h->d_exp.upload(ve) == cudaSuccess &&
+            h->d_coef.upload(vco) == cudaSuccess && h->d_mol_base.upload(h->mol_base) == cudaSuccess &&
+            h->d_mol_sbase.upload(h->mol_sbase) == cudaSuccess && h->d_mol_tbase.upload(h->mol_tbase) == cudaSuccess &&
+            h->d_mol_n.upload(h->mol_n) == cudaSuccess && h->d_mol_ns.upload(h->mol_ns) == cudaSuccess &&
+            h->d_pa.upload(h->pa) == cudaSuccess && h->d_pb.upload(h->pb) == cudaSuccess &&
+            h->d_prb.upload(h->pr_begin) == cudaSuccess && h->d_prc.upload(h->pr_count) == cudaSuccess &&
+            h->d_eoff.upload(h->e_off) == cudaSuccess && h->d_pP.alloc(npp) == cudaSuccess &&
+            h->d_pPf.alloc(npp) == cudaSuccess && h->d_E64.alloc(ne) == cudaSuccess &&
+            h->d_E32.alloc(ne) == cudaSuccess && h->d_Q.alloc(h->npair) == cudaSuccess &&
+            h->d_screen.alloc(tt) == cudaSuccess && h->d_sq.alloc(tt) == cudaSuccess &&
+            h->d_sqf.alloc(tt) == cudaSuccess && h->d_dPf.alloc(nn) == cudaSuccess &&
+            h->d_Dsh.alloc(ss) == cudaSuccess && h->d_counters.alloc(3 * MMDG_NCLASS) == cudaSuccess;
+  if (!ok) return fail(MMDG_E_NOMEM, "mmdg_set_basis: device allocation failed");
+  // ---- primitive pairs
+  {
+    PairBuildArgs a;
+    a.npair = h->npair;
+    a.pa = h->d_pa.p;
+    a.pb = h->d_pb.p;
+    a.prb = h->d_prb.p;
+    a.eoff = h->d_eoff.p;
+    a.L = h->d_L.p;
+    a.nprim = h->d_nprim.p;
+    a.poff = h->d_poff.p;
+    a.center = h->d_center.p;
+    a.exps = h->d_exp.p;
+    a.coefs = h->d_coef.p;
+    a.pP = h->d_pP.p;
+    a.pPf = h->d_pPf.p;
+    a.E64 = h->d_E64.p;
+    a.E32 = h->d_E32.p;
+    k_build_pairs<<<(h->npair + 127) / 128, 128>>>(a);
+    CUDA_TRY(cudaGetLastError());
+  }
+  // ---- Schwarz: diagonal quartets per pair class (unsorted lists)
+  std::vector<std::vector<int>> lists(kNumPairClasses);
+  for (int p = 0; p < h->npair; ++p) lists[h->pcls[p]].push_back(p);
+  CUDA_TRY(cudaMemset(h->d_Q.p, 0, sizeof(float) * h->npair));
+  CUDA_TRY(cudaMemset(h->d_screen.p, 0, sizeof(double) * (size_t)tt));
+  Geometry g = h->geom();
+  SchwarzArgs sa{h->d_screen.p, h->d_Q.p};
+  {
+    DevBuf<int> tmp[kNumPairClasses];
+    for (int c = 0; c < kNumPairClasses; ++c) {
+      if (lists[c].empty()) continue;
+      if (tmp[c].upload(lists[c]) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+      const ClassEntry* ce = nullptr;
+      for (const ClassEntry& e : kClasses)
+        if (pair_class(e.la, e.lb) == c && pair_class(e.lc, e.ld) == c) ce = &e;
+      CUDA_TRY(ce->schwarz(g, sa, tmp[c].p, (int)lists[c].size(), 0));
+    }
+    CUDA_TRY(cudaDeviceSynchronize());
+  }
+  {
+    const long long n = tt;
+    k_sqrt_screen<<<(unsigned)((n + 255) / 256), 256>>>(h->d_screen.p, h->d_sq.p, h->d_sqf.p, n);
+    CUDA_TRY(cudaGetLastError());
+  }
+  // ---- sorted class lists: primitive count ascending, Q descending
+  std::vector<float> Q(h->npair);
+  CUDA_TRY(cudaMemcpy(Q.data(), h->d_Q.p, sizeof(float) * h->npair, cudaMemcpyDeviceToHost));
+  h->cls_count.assign(kNumPairClasses, 0);
+  for (int c = 0; c < kNumPairClasses; ++c) {
+    std::vector<int>& v = lists[c];
+    std::stable_sort(v.begin(), v.end(), [&](int x, int y) {
+      if (h->pr_count[x] != h->pr_count[y]) return h->pr_count[x] < h->pr_count[y];
+      return Q[x] > Q[y];
+    });
+    h->cls_count[c] = (int)v.size();
+    if (h->d_cls[c].upload(v) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+  }
+  CUDA_TRY(cudaDeviceSynchronize());
+  h->have_basis = true;
+  return MMDG_OK;
+}
+
+extern "C" int mmdg_get_screen(mmdg_context* h, double* screen, long long n) {
+  if (!h || !screen) return fail(MMDG_E_ARG, "mmdg_get_screen: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_get_screen: no basis set");
+  if (n != h->ntot_tri) return fail(MMDG_E_ARG, "mmdg_get_screen: length must be sum N(N+1)/2");
+  DeviceGuard dg(h->device);
+  CUDA_TRY(cudaMemcpy(screen, h->d_screen.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ ERI tensor
+extern "C" int mmdg_eri_tensor(mmdg_context* h, double* out, void* stream) {
+  if (!h || !out) return fail(MMDG_E_ARG, "mmdg_eri_tensor: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_eri_tensor: no basis set");
+  if (h->nmol != 1) return fail(MMDG_E_STATE, "mmdg_eri_tensor: defined for a single molecule");
+  DeviceGuard dg(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long N = h->mol_n[0];
+  CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * N * N * N * N, st));
+  Geometry g = h->geom();
+  TensorArgs t{out};
+  for (const ClassEntry& e : kClasses) {
+    const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
+    if (!h->cls_count[cb] || !h->cls_count[ck]) continue;
+    ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, 0.f};
+    CUDA_TRY(e.tensor(g, t, cl, st));
+  }
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ Fock build
+__global__ void k_prep_density(const double* dP, float* dPf, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dPf[i] = float(fabs(dP[i]));
+}
+
+// per-molecule S x S block maxima of |dP| (one thread per shell pair block)
+__global__ void k_shell_dmax(const float* dPf, float* Dsh, const int* func, const int* L, const int* sh_mol,
+                             const int* sh_local, const long long* mol_base, const int* mol_n,
+                             const long long* mol_sbase, const int* mol_ns, int nshell) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int s1 = (int)(idx / nshell), s2 = (int)(idx % nshell);
+  if (s1 >= nshell) return;
+  const int m = sh_mol[s1];
+  if (sh_mol[s2] != m) return;
+  const int N = mol_n[m], S = mol_ns[m];
+  const float* D = dPf + mol_base[m];
+  const int n1 = (L[s1] + 1) * (L[s1] + 2) / 2, n2 = (L[s2] + 1) * (L[s2] + 2) / 2;
+  float mx = 0.f;
+  for (int a = 0; a < n1; ++a) {
+    const int i = func[s1 * kMaxComp + a];
+    if (i < 0) continue;
+    for (int b = 0; b < n2; ++b) {
+      const int j = func[s2 * kMaxComp + b];
+      if (j < 0) continue;
+      mx = fmaxf(mx, D[(long long)i * N + j]);
+    }
+  }
+  Dsh[mol_sbase[m] + (long long)sh_local[s1] * S + sh_local[s2]] = mx;
+}
+
+extern "C" int mmdg_fock(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
+                         unsigned long long* counts, void* stream) {
+  if (!h || !dP || !G) return fail(MMDG_E_ARG, "mmdg_fock: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_fock: no basis set");
+  if (!(tol >= 0.0) || !(fp32_below >= 0.0)) return fail(MMDG_E_ARG, "mmdg_fock: negative threshold");
+  DeviceGuard dgd(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nn = h->ntot_nn;
+  CUDA_TRY(cudaMemsetAsync(G, 0, sizeof(double) * nn, st));
+  CUDA_TRY(cudaMemsetAsync(h->d_counters.p, 0, sizeof(unsigned long long) * 3 * MMDG_NCLASS, st));
+  k_prep_density<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(dP, h->d_dPf.p, nn);
+  CUDA_TRY(cudaGetLastError());
+  {
+    const long long n = (long long)h->nshell * h->nshell;
+    k_shell_dmax<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->d_dPf.p, h->d_Dsh.p, h->d_func.p, h->d_L.p,
+                                                              h->d_shmol.p, h->d_shlocal.p, h->d_mol_base.p,
+                                                              h->d_mol_n.p, h->d_mol_sbase.p, h->d_mol_ns.p, h->nshell);
+    CUDA_TRY(cudaGetLastError());
+  }
+  Geometry g = h->geom();
+  FockArgs f;
+  f.dP = dP;
+  f.dPf = h->d_dPf.p;
+  f.G = G;
+  f.sq = h->d_sq.p;
+  f.sqf = h->d_sqf.p;
+  f.Dsh = h->d_Dsh.p;
+  f.tol = tol;
+  f.tolf_lo = float(tol * (1.0 - 1e-4));
+  f.tolf_hi = float(tol * (1.0 + 1e-4));
+  const float split = float(fp32_below);
+  int ci = 0;
+  for (const ClassEntry& e : kClasses) {
+    const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
+    f.counters = h->d_counters.p + 3 * ci;
+    ++ci;
+    if (!h->cls_count[cb] || !h->cls_count[ck]) continue;
+    ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, split, INFINITY};
+    CUDA_TRY(e.fock(0, g, f, cl, st));
+    if (split > 0.f) {
+      cl.qmin = 0.f;
+      cl.qmax = split;
+      CUDA_TRY(e.fock(1, g, f, cl, st));
+    }
+  }
+  if (counts) {
+    CUDA_TRY(cudaMemcpyAsync(counts, h->d_counters.p, sizeof(unsigned long long) * 3 * MMDG_NCLASS,
+                             cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ F update, Boys
+__global__ void k_fock_update(const double* G, const double* Fin, double* Fout, const long long* mol_base,
+                              const int* mol_n, int nmol, long long nn) {
+  long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= nn) return;
+  // locate the molecule block (few molecules: linear; many: binary search)
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (mol_base[mid] <= idx) lo = mid;
+    else hi = mid - 1;
+  }
+  const long long b = mol_base[lo];
+  const long long N = mol_n[lo];
+  const long long loc = idx - b, i = loc / N, j = loc % N;
+  Fout[idx] = Fin[idx] + 0.5 * (G[idx] + G[b + j * N + i]);
+}
+
+extern "C" int mmdg_fock_update(mmdg_context* h, const double* G, const double* F_in, double* F_out, void* stream) {
+  if (!h || !G || !F_in || !F_out) return fail(MMDG_E_ARG, "mmdg_fock_update: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_fock_update: no basis set");
+  if (G == F_out) return fail(MMDG_E_ARG, "mmdg_fock_update: G must not alias F_out");
+  DeviceGuard dg(h->device);
+  const long long nn = h->ntot_nn;
+  k_fock_update<<<(unsigned)((nn + 255) / 256), 256, 0, (cudaStream_t)stream>>>(G, F_in, F_out, h->d_mol_base.p,
+                                                                               h->d_mol_n.p, h->nmol, nn);
+  CUDA_TRY(cudaGetLastError());
+  return MMDG_OK;
+}
+
+template <int L>
+__global__ void k_boys(const double* tab, const double* T, double* out, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double F[L + 1];
+  boys_eval<L>(tab, T[i], F);
+  out[i] = F[L];
+}
+
+extern "C" int mmdg_boys(mmdg_context* h, int m, long long n, const double* T, double* out, void* stream) {
+  if (!h || (!T && n) || (!out && n)) return fail(MMDG_E_ARG, "mmdg_boys: null argument");
+  if (m < 0 || m > 8) return fail(MMDG_E_ARG, "mmdg_boys: order must be 0..8");
+  if (n <= 0) return MMDG_OK;
+  DeviceGuard dg(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  switch (m) {
+    case 0: k_boys<0><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 1: k_boys<1><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 2: k_boys<2><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 3: k_boys<3><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 4: k_boys<4><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 5: k_boys<5><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 6: k_boys<6><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    case 7: k_boys<7><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+    default: k_boys<8><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
+  }
+  CUDA_TRY(cudaGetLastError());
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ set screen, dense J/K
+__global__ void k_pair_q_from_screen(const double* screen, float* Q, const int* pa, const int* pb, const int* L,
+                                     const int* func, const int* sh_mol, const long long* mol_tbase, int npair) {
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= npair) return;
+  const int a = pa[pr], b = pb[pr];
+  const long long tb = mol_tbase[sh_mol[a]];
+  const int na = (L[a] + 1) * (L[a] + 2) / 2, nb = (L[b] + 1) * (L[b] + 2) / 2;
+  float q = 0.f;
+  for (int x = 0; x < na; ++x) {
+    const int i = func[a * kMaxComp + x];
+    if (i < 0) continue;
+    for (int y = 0; y < nb; ++y) {
+      int j = func[b * kMaxComp + y];
+      if (j < 0) continue;
+      int ii = i > j ? i : j, jj = i > j ? j : i;
+      q = fmaxf(q, sqrtf(fmaxf(float(screen[tb + (long long)ii * (ii + 1) / 2 + jj]), 0.f)));
+    }
+  }
+  // round up so that the shell bound stays an upper bound of the function bounds
+  Q[pr] = q * (1.0f + 1e-6f);
+}
+
+extern "C" int mmdg_set_screen(mmdg_context* h, const double* screen, long long n) {
+  if (!h || !screen) return fail(MMDG_E_ARG, "mmdg_set_screen: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_set_screen: no basis set");
+  if (n != h->ntot_tri) return fail(MMDG_E_ARG, "mmdg_set_screen: length must be sum N(N+1)/2");
+  DeviceGuard dg(h->device);
+  CUDA_TRY(cudaMemcpy(h->d_screen.p, screen, sizeof(double) * n, cudaMemcpyHostToDevice));
+  k_sqrt_screen<<<(unsigned)((n + 255) / 256), 256>>>(h->d_screen.p, h->d_sq.p, h->d_sqf.p, n);
+  CUDA_TRY(cudaGetLastError());
+  k_pair_q_from_screen<<<(h->npair + 127) / 128, 128>>>(h->d_screen.p, h->d_Q.p, h->d_pa.p, h->d_pb.p, h->d_L.p,
+                                                        h->d_func.p, h->d_shmol.p, h->d_mol_tbase.p, h->npair);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaDeviceSynchronize());
+  return MMDG_OK;
+}
+
+// J_pq = sum_rs (pq|rs) P_sr,  K_pq = sum_rs (ps|qr) P_sr   (mmd/scf.py:97-98)
+// one warp per (p,q); lanes stride over r,s
+__global__ void k_jk_dense(const double* T, const double* P, double* J, double* K, long long N) {
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= N * N) return;
+  const long long p = w / N, q = w % N;
+  double j = 0.0, k = 0.0;
+  for (long long x = lane; x < N * N; x += 32) {
+    const long long r = x / N, s = x % N;
+    const double psr = P[s * N + r];
+    j = fma(T[((p * N + q) * N + r) * N + s], psr, j);
+    k = fma(T[((p * N + s) * N + q) * N + r], psr, k);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    j += __shfl_xor_sync(0xffffffffu, j, o);
+    k += __shfl_xor_sync(0xffffffffu, k, o);
+  }
+  if (lane == 0) {
+    J[p * N + q] = j;
+    K[p * N + q] = k;
+  }
+}
+
+extern "C" int mmdg_jk_dense(mmdg_context* h, long long N, const double* T, const double* P, double* J, double* K,
+                             void* stream) {
+  if (!h || !T || !P || !J || !K || N <= 0) return fail(MMDG_E_ARG, "mmdg_jk_dense: bad argument");
+  DeviceGuard dg(h->device);
+  const long long warps = N * N;
+  k_jk_dense<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(T, P, J, K, N);
+  CUDA_TRY(cudaGetLastError());
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ one-electron integrals
+// S, T, V and the dipole integrals (cython/onee.pyx:14-192): one thread per shell
+// pair, generic loops (work O(pairs x primitives x atoms), negligible next to the
+// two-electron part).  Same formulas as the reference: overlap E_0 products
+// (onee.pyx:71-78), kinetic energy through E with l2+-2 (onee.pyx:103-133), dipole
+// E_1 + X_PC E_0 (onee.pyx:81-101), nuclear attraction 2 pi / p sum E E E R
+// (onee.pyx:175-192).
+struct OneEArgs {
+  int npair;
+  const int *pa, *pb, *L, *nprim, *poff, *func, *sh_mol;
+  const double *center, *exps, *coefs;
+  const long long* mol_base;
+  const int* mol_n;
+  const int *atom_begin, *atom_end;   // per molecule
+  const double* atom_xyz;             // [natom*3]
+  const double* atom_Z;
+  const double* origin;               // [nmol*3] dipole gauge origin (centre of nuclear charge)
+  long long nn;                       // total packed size
+  const double* boys;
+  double *S, *T, *V, *M;              // M: 3 blocks of nn
+};
+
+template <int L>
+__device__ void hermite_r_table(const double* boys, double p, double X, double Y, double Z, double* R) {
+  // R[(t*5+u)*5+v] for t+u+v <= L (L <= 4) from R^(n)_000 = (-2p)^n F_n(p |PC|^2)
+  double F[L + 1];
+  boys_eval<L>(boys, p * (X * X + Y * Y + Z * Z), F);
+  double cur[5][5][5], nxt[5][5][5];
+  double c = 1.0;
+  double R0[L + 1];
+  for (int n = 0; n <= L; ++n) {
+    R0[n] = c * F[n];
+    c *= -2.0 * p;
+  }
+  // level by level: R^(n) with t+u+v <= L-n
+  for (int t = 0; t < 5; ++t)
+    for (int u = 0; u < 5; ++u)
+      for (int v = 0; v < 5; ++v) cur[t][u][v] = 0.0;
+  cur[0][0][0] = R0[L];
+  for (int n = L - 1; n >= 0; --n) {
+    const int s = L - n;
+    for (int t = 0; t <= s; ++t)
+      for (int u = 0; u <= s - t; ++u)
+        for (int v = 0; v <= s - t - u; ++v) {
+          double val;
+          if (t + u + v == 0) val = R0[n];
+          else if (t > 0) val = X * cur[t - 1][u][v] + (t > 1 ? (t - 1) * cur[t - 2][u][v] : 0.0);
+          else if (u > 0) val = Y * cur[0][u - 1][v] + (u > 1 ? (u - 1) * cur[0][u - 2][v] : 0.0);
+          else val = Z * cur[0][0][v - 1] + (v > 1 ? (v - 1) * cur[0][0][v - 2] : 0.0);
+          nxt[t][u][v] = val;
+        }
+    for (int t = 0; t <= s; ++t)
+      for (int u = 0; u <= s - t; ++u)
+        for (int v = 0; v <= s - t - u; ++v) cur[t][u][v] = nxt[t][u][v];
+  }
+  for (int t = 0; t <= L; ++t)
+    for (int u = 0; u <= L - t; ++u)
+      for (int v = 0; v <= L - t - u; ++v) R[(t * 5 + u) * 5 + v] = cur[t][u][v];
+}
+
+__global__ void k_one_electron(OneEArgs a) {
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= a.npair) return;
+  const int sa = a.pa[pr], sb = a.pb[pr];
+  const int la = a.L[sa], lb = a.L[sb];
+  const int m = a.sh_mol[sa];
+  const long long base = a.mol_base[m];
+  const int N = a.mol_n[m];
+  const double Ax = a.center[3 * sa], Ay = a.center[3 * sa + 1], Az = a.center[3 * sa + 2];
+  const double Bx = a.center[3 * sb], By = a.center[3 * sb + 1], Bz = a.center[3 * sb + 2];
+  const double A[3] = {Ax, Ay, Az}, B[3] = {Bx, By, Bz};
+  const double AB[3] = {Ax - Bx, Ay - By, Az - Bz};
+  const double AB2 = AB[0] * AB[0] + AB[1] * AB[1] + AB[2] * AB[2];
+  const double* O = a.origin + 3 * m;
+  const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2;
+  double accS[36], accT[36], accV[36], accM[3][36];
+  for (int x = 0; x < 36; ++x) {
+    accS[x] = accT[x] = accV[x] = 0.0;
+    accM[0][x] = accM[1][x] = accM[2][x] = 0.0;
+  }
+  const double PI = 3.141592653589793238462643383279;
+  for (int ka = 0; ka < a.nprim[sa]; ++ka)
+    for (int kb = 0; kb < a.nprim[sb]; ++kb) {
+      const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+      const double p = ea + eb, ip = 1.0 / p, mu = ea * eb * ip;
+      const double P[3] = {(ea * Ax + eb * Bx) * ip, (ea * Ay + eb * By) * ip, (ea * Az + eb * Bz) * ip};
+      const double cK = a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * exp(-mu * AB2);
+      // 1D E[d][i][j][t], i <= 2, j <= lb + 2 <= 4, t <= i + j <= 6
+      double E[3][3][5][7];
+      const double i2p = 0.5 * ip;
+      for (int d = 0; d < 3; ++d) {
+        const double XPA = P[d] - A[d], XPB = P[d] - B[d];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 5; ++j)
+            for (int t = 0; t < 7; ++t) E[d][i][j][t] = 0.0;
+        E[d][0][0][0] = 1.0;
+        for (int i = 0; i < la; ++i)
+          for (int t = 0; t <= i + 1; ++t) {
+            double v = XPA * E[d][i][0][t];
+            if (t > 0) v += i2p * E[d][i][0][t - 1];
+            if (t + 1 <= i) v += (t + 1) * E[d][i][0][t + 1];
+            E[d][i + 1][0][t] = v;
+          }
+        for (int j = 0; j < lb + 2; ++j)
+          for (int i = 0; i <= la; ++i)
+            for (int t = 0; t <= i + j + 1; ++t) {
+              double v = XPB * E[d][i][j][t];
+              if (t > 0) v += i2p * E[d][i][j][t - 1];
+              if (t + 1 <= i + j) v += (t + 1) * E[d][i][j][t + 1];
+              E[d][i][j + 1][t] = v;
+            }
+      }
+      const double s3 = pow(PI * ip, 1.5) * cK;
+      // overlap, kinetic, dipole
+      int x = 0;
+      for (int xa = la; xa >= 0; --xa)
+        for (int ya = la - xa; ya >= 0; --ya) {
+          const int za = la - xa - ya;
+          for (int xb = lb; xb >= 0; --xb)
+            for (int yb = lb - xb; yb >= 0; --yb, ++x) {
+              const int zb = lb - xb - yb;
+              const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
+                                 comp_norm(zb);
+              const double Sx = E[0][xa][xb][0], Sy = E[1][ya][yb][0], Sz = E[2][za][zb][0];
+              accS[x] += nab * s3 * Sx * Sy * Sz;
+              const int lbv[3] = {xb, yb, zb};
+              const int lav[3] = {xa, ya, za};
+              double Td[3];
+              for (int d = 0; d < 3; ++d) {
+                const int l2 = lbv[d], l1 = lav[d];
+                double t = (2 * l2 + 1) * eb * E[d][l1][l2][0] - 2.0 * eb * eb * E[d][l1][l2 + 2][0];
+                if (l2 >= 2) t += -0.5 * l2 * (l2 - 1) * E[d][l1][l2 - 2][0];
+                Td[d] = t;
+              }
+              accT[x] += nab * s3 * (Td[0] * Sy * Sz + Td[1] * Sx * Sz + Td[2] * Sx * Sy);
+              const double Dx = E[0][xa][xb][1] + (P[0] - O[0]) * Sx;
+              const double Dy = E[1][ya][yb][1] + (P[1] - O[1]) * Sy;
+              const double Dz = E[2][za][zb][1] + (P[2] - O[2]) * Sz;
+              accM[0][x] += nab * s3 * Dx * Sy * Sz;
+              accM[1][x] += nab * s3 * Sx * Dy * Sz;
+              accM[2][x] += nab * s3 * Sx * Sy * Dz;
+            }
+        }
+      // nuclear attraction
+      const int L = la + lb;
+      for (int at = a.atom_begin[m]; at < a.atom_end[m]; ++at) {
+        const double C[3] = {a.atom_xyz[3 * at], a.atom_xyz[3 * at + 1], a.atom_xyz[3 * at + 2]};
+        double R[125];
+        const double X = P[0] - C[0], Y = P[1] - C[1], Z = P[2] - C[2];
+        switch (L) {
+          case 0: hermite_r_table<0>(a.boys, p, X, Y, Z, R); break;
+          case 1: hermite_r_table<1>(a.boys, p, X, Y, Z, R); break;
+          case 2: hermite_r_table<2>(a.boys, p, X, Y, Z, R); break;
+          case 3: hermite_r_table<3>(a.boys, p, X, Y, Z, R); break;
+          default: hermite_r_table<4>(a.boys, p, X, Y, Z, R); break;
+        }
+        const double pre = -a.atom_Z[at] * 2.0 * PI * ip * cK;
+        int y = 0;
+        for (int xa = la; xa >= 0; --xa)
+          for (int ya = la - xa; ya >= 0; --ya) {
+            const int za = la - xa - ya;
+            for (int xb = lb; xb >= 0; --xb)
+              for (int yb = lb - xb; yb >= 0; --yb, ++y) {
+                const int zb = lb - xb - yb;
+                const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
+                                   comp_norm(zb);
+                double v = 0.0;
+                for (int t = 0; t <= xa + xb; ++t)
+                  for (int u = 0; u <= ya + yb; ++u)
+                    for (int w = 0; w <= za + zb; ++w)
+                      v += E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][w] * R[(t * 5 + u) * 5 + w];
+                accV[y] += pre * nab * v;
+              }
+          }
+      }
+    }
+  // scatter (each function pair belongs to exactly one shell pair)
+  int x = 0;
+  for (int ca = 0; ca < na; ++ca)
+    for (int cb = 0; cb < nb; ++cb, ++x) {
+      const int i = a.func[sa * kMaxComp + ca], j = a.func[sb * kMaxComp + cb];
+      if (i < 0 || j < 0) continue;
+      const long long ij = base + (long long)i * N + j, ji = base + (long long)j * N + i;
+      a.S[ij] = accS[x];
+      a.S[ji] = accS[x];
+      a.T[ij] = accT[x];
+      a.T[ji] = accT[x];
+      a.V[ij] = accV[x];
+      a.V[ji] = accV[x];
+      for (int d = 0; d < 3; ++d) {
+        a.M[d * a.nn + ij] = accM[d][x];
+        a.M[d * a.nn + ji] = accM[d][x];
+      }
+    }
+}
+
+extern "C" int mmdg_one_electron(mmdg_context* h, int natom, const int* atom_mol, const double* atom_xyz,
+                                 const double* atom_Z, const double* origin, double* S, double* T, double* V,
+                                 double* M, void* stream) {
+  if (!h || natom < 1 || !atom_mol || !atom_xyz || !atom_Z || !origin || !S || !T || !V || !M)
+    return fail(MMDG_E_ARG, "mmdg_one_electron: bad argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_one_electron: no basis set");
+  DeviceGuard dg(h->device);
+  std::vector<int> ab(h->nmol, 0), ae(h->nmol, 0);
+  for (int i = 0; i < natom; ++i) {
+    const int m = atom_mol[i];
+    if (m < 0 || m >= h->nmol || (i > 0 && m < atom_mol[i - 1]))
+      return fail(MMDG_E_ARG, "mmdg_one_electron: atoms must be sorted by molecule");
+  }
+  for (int m = 0, i = 0; m < h->nmol; ++m) {
+    ab[m] = i;
+    while (i < natom && atom_mol[i] == m) ++i;
+    ae[m] = i;
+  }
+  DevBuf<int> d_ab, d_ae;
+  DevBuf<double> d_xyz, d_Z, d_o;
+  std::vector<double> vx(atom_xyz, atom_xyz + 3 * (size_t)natom), vZ(atom_Z, atom_Z + natom),
+      vo(origin, origin + 3 * (size_t)h->nmol);
+  if (d_ab.upload(ab) || d_ae.upload(ae) || d_xyz.upload(vx) || d_Z.upload(vZ) || d_o.upload(vo))
+    return fail(MMDG_E_NOMEM, "mmdg_one_electron: allocation");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long nn = h->ntot_nn;
+  CUDA_TRY(cudaMemsetAsync(S, 0, sizeof(double) * nn, st));
+  CUDA_TRY(cudaMemsetAsync(T, 0, sizeof(double) * nn, st));
+  CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(double) * nn, st));
+  CUDA_TRY(cudaMemsetAsync(M, 0, sizeof(double) * 3 * nn, st));
+  OneEArgs a;
+  a.npair = h->npair;
+  a.pa = h->d_pa.p;
+  a.pb = h->d_pb.p;
+  a.L = h->d_L.p;
+  a.nprim = h->d_nprim.p;
+  a.poff = h->d_poff.p;
+  a.func = h->d_func.p;
+  a.sh_mol = h->d_shmol.p;
+  a.center = h->d_center.p;
+  a.exps = h->d_exp.p;
+  a.coefs = h->d_coef.p;
+  a.mol_base = h->d_mol_base.p;
+  a.mol_n = h->d_mol_n.p;
+  a.atom_begin = d_ab.p;
+  a.atom_end = d_ae.p;
+  a.atom_xyz = d_xyz.p;
+  a.atom_Z = d_Z.p;
+  a.origin = d_o.p;
+  a.nn = nn;
+  a.boys = h->boys64.p;
+  a.S = S;
+  a.T = T;
+  a.V = V;
+  a.M = M;
+  k_one_electron<<<(h->npair + 63) / 64, 64, 0, st>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(st));  // the temporary atom buffers are freed on return
+  return MMDG_OK;
+}

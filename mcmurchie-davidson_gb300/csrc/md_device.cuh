@@ -1,0 +1,396 @@
+// md_device.cuh -- device building blocks of the McMurchie-Davidson ERI kernels.
+//
+// Numerics restate the reference (jjgoings/McMurchie-Davidson):
+//   * Boys function F_m(T) (cython/util.pxi:54-55) by tabulated Taylor interpolation
+//     plus downward recursion F_{m-1} = (2T F_m + e^{-T})/(2m-1); for T >= 36 the
+//     asymptotic F_0 = sqrt(pi/T)/2 and upward recursion F_{m+1} = ((2m+1)F_m - e^{-T})/(2T).
+//   * R^(n)_000 = (-2 alpha)^n F_n(alpha |PQ|^2) (cython/util.pxi:37-38) with the
+//     prefactor 2 pi^{5/2} / (p q sqrt(p+q)) (cython/twoe.pyx:93) folded in.
+//   * Fock digestion of one function quartet exactly as formPT (cython/fock.pyx:40-85):
+//     canonical labels i>=j, k>=l, ij>=kl; Schwarz x density screening; degeneracy
+//     s12*s34*s12_34; two Coulomb and four exchange updates of the unsymmetrised G.
+//
+// Every FP64 instruction goes through GB300's narrow FP64 pipe (measured 1.19
+// TFLOP/s against 73 TFLOP/s FP32), so integer and FP32 work is used wherever the
+// result does not need FP64: indices, screening (FP32 with a guard band; exact FP64
+// only near the threshold), table lookups.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mmdg {
+
+constexpr int kMaxComp = 6;         // Cartesian components of a d shell
+constexpr int kBoysNGrid = 576;     // T_k = k/16, k = 0..575
+constexpr int kBoysNCol = 16;       // F_0..F_14(T_k), exp(-T_k)
+constexpr double kBoysTaylorMax = 36.0 - 1.0 / 32.0;
+constexpr double kTwoPi52 = 34.986836655249725;  // 2 pi^{5/2}
+constexpr double kHalfSqrtPi = 0.88622692545275801;
+
+// ---------------------------------------------------------------------------------
+// geometry shared by every kernel
+struct Geometry {
+  // primitive pairs
+  const double4_32a* __restrict__ pP;   // (p, Px, Py, Pz) per primitive pair
+  const float4* __restrict__ pPf;   // same in FP32
+  const double* __restrict__ E64;   // E' tables, FP64
+  const float* __restrict__ E32;    // E' tables, FP32
+  // shell pairs
+  const int* __restrict__ pr_begin;  // first primitive pair
+  const int* __restrict__ pr_count;  // number of primitive pairs
+  const long long* __restrict__ e_off;  // offset of the pair's E' table (prim k at e_off + k*nnz)
+  const int* __restrict__ pa;        // shell a (la >= lb)
+  const int* __restrict__ pb;        // shell b
+  const float* __restrict__ Q;       // Schwarz bound max_{ij in ab} sqrt((ij|ij))
+  // shells
+  const int* __restrict__ func;      // [nshell*kMaxComp] molecule-local function index or -1
+  const int* __restrict__ sh_mol;    // molecule of the shell
+  const int* __restrict__ sh_local;  // molecule-local shell index
+  // molecules (packed N_m x N_m blocks; one molecule for a single system)
+  const long long* __restrict__ mol_base;    // offset of the molecule's N x N block
+  const int* __restrict__ mol_n;             // N_m
+  const long long* __restrict__ mol_sbase;   // offset of the molecule's S x S shell block
+  const int* __restrict__ mol_ns;            // S_m
+  const long long* __restrict__ mol_tbase;   // offset of the molecule's N(N+1)/2 pair table
+  // Boys tables
+  const double* __restrict__ boys64;  // [kBoysNGrid*kBoysNCol]
+  const float* __restrict__ boys32;
+};
+
+// ---------------------------------------------------------------------------------
+// Boys function: Fn[0..L] at T
+template <int L>
+__device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double T, double* Fn) {
+  if (T < kBoysTaylorMax) {
+    int k = __double2int_rn(T * 16.0);
+    k = min(max(k, 0), kBoysNGrid - 1);
+    const double* __restrict__ row = tab + k * kBoysNCol;
+    const double y = fma(double(k), 0.0625, -T);  // -(T - T_k), |y| <= 1/32
+    const double y2 = y * 0.5, y3 = y * (1.0 / 3.0), y4 = y * 0.25, y5 = y * 0.2, y6 = y * (1.0 / 6.0);
+    // F_L(T) = sum_{n=0}^{6} F_{L+n}(T_k) y^n / n!  (Horner in y/n)
+    double f = row[L + 6];
+    f = fma(f, y6, row[L + 5]);
+    f = fma(f, y5, row[L + 4]);
+    f = fma(f, y4, row[L + 3]);
+    f = fma(f, y3, row[L + 2]);
+    f = fma(f, y2, row[L + 1]);
+    f = fma(f, y, row[L]);
+    Fn[L] = f;
+    if (L > 0) {
+      // exp(-T) = exp(-T_k) * exp(y), Taylor to y^7 / 7!
+      const double y7 = y * (1.0 / 7.0);
+      double e = fma(y7, 1.0, 1.0);
+      e = fma(e, y6, 1.0);
+      e = fma(e, y5, 1.0);
+      e = fma(e, y4, 1.0);
+      e = fma(e, y3, 1.0);
+      e = fma(e, y2, 1.0);
+      e = fma(e, y, 1.0);
+      const double eT = e * row[kBoysNCol - 1];
+      const double T2 = T + T;
+#pragma unroll
+      for (int m = L; m > 0; --m) Fn[m - 1] = fma(T2, Fn[m], eT) * (1.0 / double(2 * m - 1));
+    }
+  } else {
+    const double rs = rsqrt(T);
+    Fn[0] = kHalfSqrtPi * rs;
+    if (L > 0) {
+      const double eTh = 0.5 * exp(-T);
+      const double iT = rs * rs;
+#pragma unroll
+      for (int m = 0; m < L; ++m) Fn[m + 1] = fma(double(m) + 0.5, Fn[m], -eTh) * iT;
+    }
+  }
+}
+
+template <int L>
+__device__ __forceinline__ void boys_eval(const float* __restrict__ tab, float T, float* Fn) {
+  if (T < float(kBoysTaylorMax)) {
+    int k = __float2int_rn(T * 16.0f);
+    k = min(max(k, 0), kBoysNGrid - 1);
+    const float* __restrict__ row = tab + k * kBoysNCol;
+    const float y = fmaf(float(k), 0.0625f, -T);
+    const float y2 = y * 0.5f, y3 = y * (1.0f / 3.0f), y4 = y * 0.25f;
+    float f = row[L + 4];
+    f = fmaf(f, y4, row[L + 3]);
+    f = fmaf(f, y3, row[L + 2]);
+    f = fmaf(f, y2, row[L + 1]);
+    f = fmaf(f, y, row[L]);
+    Fn[L] = f;
+    if (L > 0) {
+      const float y5 = y * 0.2f;
+      float e = fmaf(y5, 1.0f, 1.0f);
+      e = fmaf(e, y4, 1.0f);
+      e = fmaf(e, y3, 1.0f);
+      e = fmaf(e, y2, 1.0f);
+      e = fmaf(e, y, 1.0f);
+      const float eT = e * row[kBoysNCol - 1];
+      const float T2 = T + T;
+#pragma unroll
+      for (int m = L; m > 0; --m) Fn[m - 1] = fmaf(T2, Fn[m], eT) * (1.0f / float(2 * m - 1));
+    }
+  } else {
+    const float rs = rsqrtf(T);
+    Fn[0] = float(kHalfSqrtPi) * rs;
+    if (L > 0) {
+      const float eTh = 0.5f * expf(-T);
+      const float iT = rs * rs;
+#pragma unroll
+      for (int m = 0; m < L; ++m) Fn[m + 1] = fmaf(float(m) + 0.5f, Fn[m], -eTh) * iT;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// per-quartet context handed to the generated class code
+template <typename Real>
+struct Ctx;
+
+template <>
+struct Ctx<double> {
+  const Geometry* g;
+  int bra_begin, bra_end, ket_begin, ket_end;
+  long long ebra, eket;
+  int nnz_ab, nnz_cd;
+  double* rs;
+  int rstr;
+
+  template <typename R>
+  __device__ __forceinline__ R* rsmem() const { return reinterpret_cast<R*>(rs); }
+  __device__ __forceinline__ int rstride() const { return rstr; }
+  __device__ __forceinline__ const double* ket_E(int j) const {
+    return g->E64 + eket + (long long)(j - ket_begin) * nnz_cd;
+  }
+  __device__ __forceinline__ const double* bra_E(int i) const {
+    return g->E64 + ebra + (long long)(i - bra_begin) * nnz_ab;
+  }
+  template <int L>
+  __device__ __forceinline__ void hermite_r0(int i, int j, double* Rn, double& X, double& Y, double& Z) const {
+    const double4_32a a = g->pP[i];
+    const double4_32a b = g->pP[j];
+    X = a.y - b.y;
+    Y = a.z - b.z;
+    Z = a.w - b.w;
+    const double r2 = fma(X, X, fma(Y, Y, Z * Z));
+    const double rsum = rsqrt(a.x + b.x);
+    const double alpha = a.x * b.x * (rsum * rsum);
+    double F[L + 1];
+    boys_eval<L>(g->boys64, alpha * r2, F);
+    double c = kTwoPi52 * rsum;
+    const double m2a = -2.0 * alpha;
+#pragma unroll
+    for (int n = 0; n <= L; ++n) {
+      Rn[n] = c * F[n];
+      c *= m2a;
+    }
+  }
+};
+
+template <>
+struct Ctx<float> {
+  const Geometry* g;
+  int bra_begin, bra_end, ket_begin, ket_end;
+  long long ebra, eket;
+  int nnz_ab, nnz_cd;
+  float* rs;
+  int rstr;
+
+  template <typename R>
+  __device__ __forceinline__ R* rsmem() const { return reinterpret_cast<R*>(rs); }
+  __device__ __forceinline__ int rstride() const { return rstr; }
+  __device__ __forceinline__ const float* ket_E(int j) const {
+    return g->E32 + eket + (long long)(j - ket_begin) * nnz_cd;
+  }
+  __device__ __forceinline__ const float* bra_E(int i) const {
+    return g->E32 + ebra + (long long)(i - bra_begin) * nnz_ab;
+  }
+  template <int L>
+  __device__ __forceinline__ void hermite_r0(int i, int j, float* Rn, float& X, float& Y, float& Z) const {
+    // P - Q in FP64 (coordinates of ~10 bohr would lose the difference in FP32)
+    const double4_32a a = g->pP[i];
+    const double4_32a b = g->pP[j];
+    X = float(a.y - b.y);
+    Y = float(a.z - b.z);
+    Z = float(a.w - b.w);
+    const float4 af = g->pPf[i];
+    const float4 bf = g->pPf[j];
+    const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
+    const float rsum = rsqrtf(af.x + bf.x);
+    const float alpha = af.x * bf.x * (rsum * rsum);
+    float F[L + 1];
+    boys_eval<L>(g->boys32, alpha * r2, F);
+    float c = float(kTwoPi52) * rsum;
+    const float m2a = -2.0f * alpha;
+#pragma unroll
+    for (int n = 0; n <= L; ++n) {
+      Rn[n] = c * F[n];
+      c *= m2a;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------------
+// shell-quartet description shared by the digests
+struct QuartetInfo {
+  int sa, sb, sc, sd;        // shells (bra pair a>=b in L, ket pair c>=d in L)
+  bool same_ab, same_cd, same_pair;
+  int mol;
+};
+
+__device__ __forceinline__ int tri(int i) { return i * (i + 1) / 2; }
+
+// Fock (formPT) digest --------------------------------------------------------------
+struct FockArgs {
+  const double* dP;      // packed per-molecule N x N (density difference)
+  const float* dPf;      // FP32 copy of |dP| for screening
+  double* G;             // packed per-molecule N x N, accumulated (unsymmetrised)
+  const double* sq;      // sqrt(screen) per molecule-local function pair, packed N(N+1)/2
+  const float* sqf;      // FP32 copy
+  const float* Dsh;      // per-molecule S x S shell-block max |dP|
+  double tol;
+  float tolf_lo, tolf_hi;  // FP32 guard band around tol
+  unsigned long long* counters;  // [0] computed function quartets, [1] computed shell quartets
+};
+
+template <int NB, int ND>
+struct FockDigest {
+  const Geometry& g;
+  const FockArgs& f;
+  QuartetInfo q;
+  long long base;
+  long long tbase;
+  int N;
+  unsigned int nfq;
+
+  __device__ __forceinline__ FockDigest(const Geometry& g_, const FockArgs& f_, const QuartetInfo& q_)
+      : g(g_), f(f_), q(q_), nfq(0) {
+    base = g.mol_base[q.mol];
+    tbase = g.mol_tbase[q.mol];
+    N = g.mol_n[q.mol];
+  }
+
+  template <typename Real>
+  __device__ __forceinline__ void put(int ca, int cb, int cc, int cd, Real vr) {
+    if (q.same_ab && ca < cb) return;
+    if (q.same_cd && cc < cd) return;
+    if (q.same_pair && (ca * NB + cb) < (cc * ND + cd)) return;
+    int i = __ldg(g.func + q.sa * kMaxComp + ca);
+    int j = __ldg(g.func + q.sb * kMaxComp + cb);
+    int k = __ldg(g.func + q.sc * kMaxComp + cc);
+    int l = __ldg(g.func + q.sd * kMaxComp + cd);
+    if ((i | j | k | l) < 0) return;
+    if (i < j) { int t = i; i = j; j = t; }
+    if (k < l) { int t = k; k = l; l = t; }
+    int ij = tri(i) + j, kl = tri(k) + l;
+    if (ij < kl) {
+      int t = i; i = k; k = t;
+      t = j; j = l; l = t;
+      t = ij; ij = kl; kl = t;
+    }
+    const long long rI = base + (long long)i * N, rJ = base + (long long)j * N;
+    const long long rK = base + (long long)k * N;
+    // screening: sqrt(screen[ij]) sqrt(screen[kl]) max(4|dP_ij|,4|dP_kl|,|dP_ik|,|dP_il|,|dP_jk|,|dP_jl|) < tol
+    {
+      float dm = fmaxf(4.0f * fmaxf(__ldg(f.dPf + rI + j), __ldg(f.dPf + rK + l)),
+                       fmaxf(fmaxf(__ldg(f.dPf + rI + k), __ldg(f.dPf + rI + l)),
+                             fmaxf(__ldg(f.dPf + rJ + k), __ldg(f.dPf + rJ + l))));
+      const float bf = __ldg(f.sqf + tbase + ij) * __ldg(f.sqf + tbase + kl) * dm;
+      if (bf < f.tolf_lo) return;
+      if (bf < f.tolf_hi) {  // near the threshold: the reference's test in FP64
+        const double* dP = f.dP;
+        double d = fmax(4.0 * fmax(fabs(dP[rI + j]), fabs(dP[rK + l])),
+                        fmax(fmax(fabs(dP[rI + k]), fabs(dP[rI + l])), fmax(fabs(dP[rJ + k]), fabs(dP[rJ + l]))));
+        if (f.sq[tbase + ij] * f.sq[tbase + kl] * d < f.tol) return;
+      }
+    }
+    double v = double(vr);
+    // degeneracy s12 * s34 * s12_34 (fock.pyx:60-70); powers of two
+    if (i != j) v += v;
+    if (k != l) v += v;
+    if (!(i == k && j == l)) v += v;
+    const double* dP = f.dP;
+    double* G = f.G;
+    const long long rL = base + (long long)l * N;
+    atomicAdd(G + rI + j, dP[rK + l] * v);
+    atomicAdd(G + rK + l, dP[rI + j] * v);
+    const double vq = -0.25 * v;
+    atomicAdd(G + rI + k, dP[rJ + l] * vq);
+    atomicAdd(G + rJ + l, dP[rI + k] * vq);
+    atomicAdd(G + rI + l, dP[rJ + k] * vq);
+    atomicAdd(G + rK + j, dP[rI + l] * vq);
+    (void)rL;
+    ++nfq;
+  }
+};
+
+// ERI tensor digest (doERIs, twoe.pyx:12-31): the eight symmetric copies -----------
+struct TensorArgs {
+  double* out;  // N^4 of molecule 0
+};
+
+template <int NB, int ND>
+struct TensorDigest {
+  const Geometry& g;
+  const TensorArgs& t;
+  QuartetInfo q;
+  long long N;
+  __device__ __forceinline__ TensorDigest(const Geometry& g_, const TensorArgs& t_, const QuartetInfo& q_)
+      : g(g_), t(t_), q(q_) {
+    N = g.mol_n[q.mol];
+  }
+  template <typename Real>
+  __device__ __forceinline__ void put(int ca, int cb, int cc, int cd, Real vr) {
+    if (q.same_ab && ca < cb) return;
+    if (q.same_cd && cc < cd) return;
+    if (q.same_pair && (ca * NB + cb) < (cc * ND + cd)) return;
+    const long long i = __ldg(g.func + q.sa * kMaxComp + ca);
+    const long long j = __ldg(g.func + q.sb * kMaxComp + cb);
+    const long long k = __ldg(g.func + q.sc * kMaxComp + cc);
+    const long long l = __ldg(g.func + q.sd * kMaxComp + cd);
+    if ((i | j | k | l) < 0) return;
+    const double v = double(vr);
+    double* o = t.out;
+    o[((i * N + j) * N + k) * N + l] = v;
+    o[((k * N + l) * N + i) * N + j] = v;
+    o[((j * N + i) * N + l) * N + k] = v;
+    o[((l * N + k) * N + j) * N + i] = v;
+    o[((j * N + i) * N + k) * N + l] = v;
+    o[((l * N + k) * N + i) * N + j] = v;
+    o[((i * N + j) * N + l) * N + k] = v;
+    o[((k * N + l) * N + j) * N + i] = v;
+  }
+};
+
+// Schwarz digest (Molecule.build screen dict, molecule.py:95-99) ---------------------
+struct SchwarzArgs {
+  double* screen;  // packed per-molecule N(N+1)/2: (ij|ij)
+  float* Qpair;    // per shell pair: max sqrt((ij|ij)), written via atomicMax on the bits
+};
+
+template <int NB, int ND>
+struct SchwarzDigest {
+  const Geometry& g;
+  const SchwarzArgs& s;
+  QuartetInfo q;
+  int pair;
+  long long tbase;
+  __device__ __forceinline__ SchwarzDigest(const Geometry& g_, const SchwarzArgs& s_, const QuartetInfo& q_, int pair_)
+      : g(g_), s(s_), q(q_), pair(pair_) {
+    tbase = g.mol_tbase[q.mol];
+  }
+  template <typename Real>
+  __device__ __forceinline__ void put(int ca, int cb, int cc, int cd, Real vr) {
+    if (ca != cc || cb != cd) return;
+    if (q.same_ab && ca < cb) return;
+    int i = __ldg(g.func + q.sa * kMaxComp + ca);
+    int j = __ldg(g.func + q.sb * kMaxComp + cb);
+    if ((i | j) < 0) return;
+    if (i < j) { int t = i; i = j; j = t; }
+    const double v = double(vr);
+    s.screen[tbase + tri(i) + j] = v;
+    const float r = sqrtf(fmaxf(float(v), 0.0f));
+    atomicMax(reinterpret_cast<int*>(s.Qpair + pair), __float_as_int(r));
+  }
+};
+
+}  // namespace mmdg

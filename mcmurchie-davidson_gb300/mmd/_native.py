@@ -1,0 +1,207 @@
+"""ctypes binding of ``libmmdg.so`` (include/mmdg.h) and the per-basis device context.
+
+The GPU path has no CPU fallback: if the library is missing or no CUDA device is
+visible, every call raises ``MMDGError``.  Device buffers are torch tensors (torch
+is used for device memory and streams only); their ``data_ptr()`` crosses the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmmdg.so")
+NCLASS = 21
+MAX_COMP = 6
+LMAX = 2
+
+_lib = None
+_lock = threading.Lock()
+
+
+class MMDGError(RuntimeError):
+    pass
+
+
+def _bind(L):
+    c_int, c_ll, c_d, p = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
+    sig = {
+        "mmdg_last_error": (ctypes.c_char_p, []),
+        "mmdg_create": (c_int, [ctypes.POINTER(p), c_int]),
+        "mmdg_destroy": (c_int, [p]),
+        "mmdg_set_basis": (c_int, [p, c_int, p, c_int, p, p, p, p, p, p, p]),
+        "mmdg_get_screen": (c_int, [p, p, c_ll]),
+        "mmdg_set_screen": (c_int, [p, p, c_ll]),
+        "mmdg_eri_tensor": (c_int, [p, p, p]),
+        "mmdg_fock": (c_int, [p, p, p, c_d, c_d, p, p]),
+        "mmdg_boys": (c_int, [p, c_int, c_ll, p, p, p]),
+        "mmdg_fock_update": (c_int, [p, p, p, p, p]),
+        "mmdg_jk_dense": (c_int, [p, c_ll, p, p, p, p, p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def lib():
+    """Load libmmdg.so (build it with ``mcmurchie-davidson_gb300/build.py`` first)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise MMDGError(f"{LIB_PATH} not built: run mcmurchie-davidson_gb300/build.py "
+                                "(the GPU path has no CPU fallback)")
+            _lib = _bind(ctypes.CDLL(LIB_PATH))
+    return _lib
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        msg = lib().mmdg_last_error().decode(errors="replace")
+        raise MMDGError(f"{what} failed ({rc}): {msg}")
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise MMDGError("no CUDA device visible: the two-electron path runs only on the GPU")
+    return torch
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def stream_ptr(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Context:
+    """One device context holding the primitive-pair data of a basis (one or many molecules).
+
+    ``shells`` is a ``ShellSet`` (``mmd.integrals.shells``) or a list of them (a
+    batch of molecules)."""
+
+    def __init__(self, shells, device: int | None = None):
+        torch = _torch()
+        self.torch = torch
+        self.device = torch.cuda.current_device() if device is None else int(device)
+        h = ctypes.c_void_p()
+        check(lib().mmdg_create(ctypes.byref(h), self.device), "mmdg_create")
+        self._h = h
+        sets = shells if isinstance(shells, (list, tuple)) else [shells]
+        self.sets = list(sets)
+        self.nmol = len(sets)
+        self.nfunc = np.array([s.nfunc for s in sets], dtype=np.int32)
+        mol = np.concatenate([np.full(s.nshell, m, dtype=np.int32) for m, s in enumerate(sets)])
+        L = np.concatenate([s.L for s in sets]).astype(np.int32)
+        K = np.concatenate([s.nprim for s in sets]).astype(np.int32)
+        cen = np.ascontiguousarray(np.concatenate([s.center for s in sets]), dtype=np.float64)
+        ex = np.ascontiguousarray(np.concatenate([s.exps for s in sets]), dtype=np.float64)
+        co = np.ascontiguousarray(np.concatenate([s.coefs for s in sets]), dtype=np.float64)
+        fn = np.ascontiguousarray(np.concatenate([s.func for s in sets]), dtype=np.int32)
+        self.nshell = len(L)
+        self._keep = (mol, L, K, cen, ex, co, fn)
+        with torch.cuda.device(self.device):
+            check(lib().mmdg_set_basis(h, self.nmol, _ptr(self.nfunc), self.nshell, _ptr(mol), _ptr(L), _ptr(K),
+                                       _ptr(cen), _ptr(ex), _ptr(co), _ptr(fn)), "mmdg_set_basis")
+        self.nn = int(np.sum(self.nfunc.astype(np.int64) ** 2))
+        self.ntri = int(np.sum(self.nfunc.astype(np.int64) * (self.nfunc + 1) // 2))
+        self.base = np.concatenate([[0], np.cumsum(self.nfunc.astype(np.int64) ** 2)[:-1]])
+        self.tbase = np.concatenate([[0], np.cumsum(self.nfunc.astype(np.int64) * (self.nfunc + 1) // 2)[:-1]])
+        self.last_counts = None
+        self._user_screen = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mmdg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- Schwarz table
+    def screen(self) -> np.ndarray:
+        out = np.zeros(self.ntri)
+        check(lib().mmdg_get_screen(self._h, _ptr(out), self.ntri), "mmdg_get_screen")
+        return out
+
+    def set_screen(self, screen: np.ndarray) -> None:
+        s = np.ascontiguousarray(screen, dtype=np.float64)
+        if s.size != self.ntri:
+            raise ValueError("screen table has the wrong length")
+        check(lib().mmdg_set_screen(self._h, _ptr(s), self.ntri), "mmdg_set_screen")
+
+    # -------------------------------------------------------------- integrals
+    def eri_tensor(self, out=None):
+        torch = self.torch
+        if self.nmol != 1:
+            raise MMDGError("eri_tensor is defined for a single molecule")
+        N = int(self.nfunc[0])
+        if out is None:
+            out = torch.empty((N, N, N, N), dtype=torch.float64, device=f"cuda:{self.device}")
+        check(lib().mmdg_eri_tensor(self._h, ctypes.c_void_p(out.data_ptr()), stream_ptr()), "mmdg_eri_tensor")
+        return out
+
+    def fock(self, dP, G=None, tol: float = 1e-12, fp32_below: float = 0.0, counts: bool = False):
+        """Unsymmetrised G(dP) (formPT semantics); dP/G are packed device float64 tensors."""
+        torch = self.torch
+        if dP.dtype != torch.float64 or not dP.is_cuda or not dP.is_contiguous() or dP.numel() != self.nn:
+            raise ValueError("dP must be a contiguous CUDA float64 tensor of sum N_m^2 elements")
+        if G is None:
+            G = torch.empty_like(dP)
+        cnt = np.zeros(3 * NCLASS, dtype=np.uint64) if counts else None
+        check(lib().mmdg_fock(self._h, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(G.data_ptr()), float(tol),
+                              float(fp32_below), _ptr(cnt) if counts else None, stream_ptr()), "mmdg_fock")
+        if counts:
+            self.last_counts = cnt.reshape(NCLASS, 3)
+        return G
+
+    def fock_update(self, G, F_in, F_out):
+        check(lib().mmdg_fock_update(self._h, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(F_in.data_ptr()),
+                                     ctypes.c_void_p(F_out.data_ptr()), stream_ptr()), "mmdg_fock_update")
+        return F_out
+
+    def jk_dense(self, T, P, J, K):
+        N = P.shape[-1]
+        check(lib().mmdg_jk_dense(self._h, N, ctypes.c_void_p(T.data_ptr()), ctypes.c_void_p(P.data_ptr()),
+                                  ctypes.c_void_p(J.data_ptr()), ctypes.c_void_p(K.data_ptr()), stream_ptr()),
+              "mmdg_jk_dense")
+        return J, K
+
+    def boys(self, m: int, T):
+        out = self.torch.empty_like(T)
+        check(lib().mmdg_boys(self._h, int(m), T.numel(), ctypes.c_void_p(T.data_ptr()),
+                              ctypes.c_void_p(out.data_ptr()), stream_ptr()), "mmdg_boys")
+        return out
+
+
+_default_ctx = None
+
+
+def scratch_context():
+    """A context without basis (for mmdg_boys / mmdg_jk_dense)."""
+    global _default_ctx
+    torch = _torch()
+    if _default_ctx is None:
+        class _Bare:
+            pass
+        b = _Bare()
+        h = ctypes.c_void_p()
+        check(lib().mmdg_create(ctypes.byref(h), torch.cuda.current_device()), "mmdg_create")
+        b._h = h
+        b.torch = torch
+        b.boys = lambda m, T: Context.boys(b, m, T)
+        b.jk_dense = lambda T, P, J, K: Context.jk_dense(b, T, P, J, K)
+        _default_ctx = b
+    return _default_ctx

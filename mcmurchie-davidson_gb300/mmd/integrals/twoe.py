@@ -1,0 +1,104 @@
+"""Two-electron integrals on the GPU, behind the reference's ``mmd.integrals.twoe`` API.
+
+``Basis``, ``ERI`` and ``doERIs`` keep the signatures and semantics of
+cython/basis.pxi:6-121 and cython/twoe.pyx:12-50.  The integrals themselves are
+evaluated by the sm_103a McMurchie-Davidson kernels of libmmdg.so; there is no
+CPU path.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .. import _native
+from .shells import fingerprint, shells_from_bfs
+
+PI = 3.141592653589793238462643383279  # cython/util.pxi:7
+
+
+def _fact2(k: int) -> float:
+    """(2n-1)!! with (-1)!! = 1, the value the reference's normalisation assumes."""
+    r = 1.0
+    while k > 1:
+        r *= k
+        k -= 2
+    return r
+
+
+class Basis:
+    """Contracted Cartesian Gaussian function (cython/basis.pxi:6-121).
+
+    Same constructor and attributes as the reference's extension class:
+    ``Basis(origin, shell, num_exps, exps, coefs)`` with ``origin``, ``shell``,
+    ``num_exps``, ``exps``, ``coefs`` (contraction-normalised in place) and
+    ``norm`` (primitive normalisation)."""
+
+    __slots__ = ("origin", "shell", "num_exps", "exps", "coefs", "norm")
+
+    def __init__(self, origin, shell, num_exps, exps, coefs):
+        self.origin = np.array(origin, dtype=np.float64).reshape(3)
+        self.shell = np.array(shell, dtype=np.int64).reshape(3)
+        self.num_exps = int(num_exps)
+        if self.num_exps < 1:
+            raise ValueError("a basis function needs at least one primitive")
+        self.exps = np.array(exps, dtype=np.float64)[: self.num_exps].copy()
+        self.coefs = np.array(coefs, dtype=np.float64)[: self.num_exps].copy()
+        self.norm = np.zeros(self.num_exps)
+        self.normalize()
+
+    def normalize(self):
+        """Primitive then contracted normalisation (basis.pxi:87-120)."""
+        l, m, n = (int(x) for x in self.shell)
+        L = l + m + n
+        f2 = _fact2(2 * l - 1) * _fact2(2 * m - 1) * _fact2(2 * n - 1)
+        self.norm = np.sqrt(np.power(2, 2 * L + 1.5) * np.power(self.exps, L + 1.5) / f2 / np.power(np.pi, 1.5))
+        prefactor = np.power(np.pi, 1.5) * f2 / np.power(2.0, L)
+        N = 0.0
+        for ia in range(self.num_exps):
+            for ib in range(self.num_exps):
+                N += self.norm[ia] * self.norm[ib] * self.coefs[ia] * self.coefs[ib] / \
+                    np.power(self.exps[ia] + self.exps[ib], L + 1.5)
+        N *= prefactor
+        N = np.power(N, -0.5)
+        self.coefs *= N
+        return self.norm
+
+
+_ctx_cache: dict = {}
+
+
+def context_for(bfs):
+    """Device context (primitive pairs + Schwarz table) for a basis list, cached."""
+    key = fingerprint(bfs)
+    ctx = _ctx_cache.get(key)
+    if ctx is None:
+        if len(_ctx_cache) > 8:
+            _ctx_cache.clear()
+        ctx = _native.Context(shells_from_bfs(bfs))
+        _ctx_cache[key] = ctx
+    return ctx
+
+
+def ERI(a, b, c, d) -> float:
+    """Contracted ERI (ab|cd) of four basis functions (twoe.pyx:36-50)."""
+    ctx = _native.Context(shells_from_bfs([a, b, c, d]))
+    T = ctx.eri_tensor()
+    v = float(T[0, 1, 2, 3].item())
+    ctx.close()
+    return v
+
+
+def doERIs(N, TwoE, bfs):
+    """Fill ``TwoE`` (N^4, C order) with all ERIs and return it (twoe.pyx:12-31)."""
+    N = int(N)
+    if len(bfs) != N:
+        raise ValueError("doERIs: N must equal len(bfs)")
+    ctx = context_for(bfs)
+    T = ctx.eri_tensor()
+    out = T.cpu().numpy()
+    TwoE[...] = out
+    return TwoE
+
+
+def eri_tensor_device(bfs):
+    """The ERI tensor as a CUDA tensor (kept on the device for the conventional SCF)."""
+    return context_for(bfs).eri_tensor()

@@ -1,0 +1,236 @@
+"""RHF driver (mmd/scf.py) with the two-electron work on the GPU.
+
+``RHF(doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12)`` keeps the
+reference's algorithm step for step (mmd/scf.py:10-80):
+
+* start from P = 0, F = Core (core-Hamiltonian guess);
+* direct SCF: incremental Fock build F = F_old + sym(G(P - P_old)) with G from the
+  formPT kernel (Schwarz x density screening at ``acc2e``), never reset;
+  conventional: F = Core + 2J - K from the ERI tensor;
+* 8-deep DIIS on X (FPS - SPF) X, eigensolve of X^T F X, P = C_occ C_occ^T,
+  E = tr((Core + F) P) + E_nuc, stop when ||P - P_old||_F < ``conver``.
+
+Every matrix stays on the device (float64): the Fock update runs in libmmdg.so,
+DIIS / eigensolve / products in cuBLAS / cuSOLVER through torch.  Extra keyword
+arguments (all default to the reference's behaviour):
+
+* ``fp32_below``  Schwarz-bound threshold under which shell quartets run in FP32
+  (0: plain FP64 method);
+* ``guess``       initial density (N x N array) instead of P = 0, with a full first
+  Fock build F = Core + sym(G(P_guess));
+* ``guess_fallback``  with a guess: revert to the core guess when the DIIS error
+  grows for 3 consecutive iterations;
+* ``maxiter``     iteration cap (reference: 100).
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+
+class SCF(object):
+    """SCF methods for the molecule object (mmd/scf.py:8-180)."""
+
+    def RHF(self, doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12, fp32_below=0.0, guess=None,
+            guess_fallback=True, maxiter=100, _timings=None):
+        self.is_converged = False
+        self.delta_energy = 1e20
+        self.P_RMS = 1e20
+        self.maxiter = int(maxiter)
+        self.direct = direct
+        if self.direct:
+            self.incFockRst = False
+        self.scrTol = acc2e
+        self.fp32_below = float(fp32_below)
+        self.build(self.direct)
+        ctx = self.context
+        torch = ctx.torch
+        N = self.nbasis
+        dev = self._dev["S"].device
+        dd = self._dev
+        Core, X, S = dd["Core"], dd["X"], dd["S"]
+        if not self.direct:
+            self._TwoE_dev = dd["TwoE"]
+        self.fock_builds = 0
+        self.fock_time = 0.0
+        self.guess_used = guess is not None
+        self.guess_reverted = False
+
+        P_old = torch.zeros((N, N), dtype=torch.float64, device=dev)
+        P = P_old
+        F = Core.clone()
+        if guess is not None:
+            Pg = torch.as_tensor(np.asarray(guess, dtype=np.float64), device=dev)
+            G = self._two_electron(Pg, torch.zeros_like(Pg))
+            F = Core + G
+            P_old = Pg
+            P = Pg
+        fockSet, errorSet = [], []
+        energy = None
+        FO = None
+        err_hist = []
+        t_start = time.perf_counter()
+        for step in range(self.maxiter):
+            if step > 0:
+                F_old = F
+                energy_old = energy
+                if self.direct:
+                    G = self._two_electron(P, P_old)
+                    F = torch.empty_like(F_old)
+                    ctx.fock_update(G, F_old, F)
+                else:
+                    F = self._conventional_fock(P)
+                P_old = P
+                if DIIS:
+                    F_diis, derr = self._diis(F, P, S, X, fockSet, errorSet)
+                    FO = X.T @ F_diis @ X
+                    err_hist.append(derr)
+                    if (self.guess_used and guess_fallback and not self.guess_reverted and len(err_hist) >= 4
+                            and err_hist[-1] > err_hist[-2] > err_hist[-3] > err_hist[-4]):
+                        # learned/initial guess misbehaves: restart from the core guess
+                        self.guess_reverted = True
+                        P_old = torch.zeros_like(P)
+                        F = Core.clone()
+                        fockSet.clear()
+                        errorSet.clear()
+                        FO = X.T @ F @ X
+            if not DIIS or step == 0:
+                FO = X.T @ F @ X
+            E, CO = torch.linalg.eigh(FO)
+            C = X @ CO
+            Cocc = C[:, : self.nocc]
+            P = Cocc @ Cocc.T
+            energy = float(torch.sum((Core + F) * P.T).item()) + self.nuc_energy
+            if step > 0:
+                self.delta_energy = energy - energy_old
+                self.P_RMS = float(torch.linalg.norm(P - P_old).item())
+            if np.abs(self.P_RMS) < conver or step == (self.maxiter - 1):
+                if step == (self.maxiter - 1):
+                    print("NOT CONVERGED")
+                else:
+                    self.is_converged = True
+                self.iterations = step
+                break
+        self.scf_time = time.perf_counter() - t_start
+        # results back to the reference's attribute names (host arrays)
+        self.P = P.cpu().numpy()
+        self.P_old = P_old.cpu().numpy()
+        self.F = F.cpu().numpy()
+        self.FO = FO.cpu().numpy()
+        self.C = C.cpu().numpy()
+        self.CO = CO.cpu().numpy()
+        self.MO = E.cpu().numpy()
+        self.energy = np.float64(energy)
+        self.el_energy = self.energy - self.nuc_energy
+        if self.is_converged:
+            FPS = self.F @ self.P @ self.S
+            error = FPS - FPS.T
+            self.computeDipole()
+            if doPrint:
+                print("E(SCF)    = ", "{0:.12f}".format(self.energy.real) + " in " + str(step) + " iterations")
+                print("  Convergence:")
+                print("    FPS-SPF  = ", np.linalg.norm(error))
+                print("    RMS(P)   = ", "{0:.2e}".format(self.P_RMS))
+                print("    dE(SCF)  = ", "{0:.2e}".format(self.delta_energy))
+                print("  Dipole X = ", "{0:.8f}".format(self.mu[0].real))
+                print("  Dipole Y = ", "{0:.8f}".format(self.mu[1].real))
+                print("  Dipole Z = ", "{0:.8f}".format(self.mu[2].real))
+        return self.energy
+
+    # ---------------------------------------------------------------- pieces
+    def _two_electron(self, P, P_old):
+        """Unsymmetrised G(P - P_old) on the GPU, symmetrised: (G + G^T)/2."""
+        ctx = self.context
+        t0 = time.perf_counter()
+        dP = (P - P_old).contiguous().view(-1)
+        G = ctx.fock(dP, tol=self.scrTol, fp32_below=self.fp32_below)
+        self.fock_builds += 1
+        self.fock_time += time.perf_counter() - t0
+        G = G.view(self.nbasis, self.nbasis)
+        return 0.5 * (G + G.T)
+
+    def _conventional_fock(self, P):
+        ctx = self.context
+        torch = ctx.torch
+        J = torch.empty_like(P)
+        K = torch.empty_like(P)
+        ctx.jk_dense(self._TwoE_dev, P.contiguous(), J, K)
+        self.fock_builds += 1
+        return self._dev["Core"] + 2.0 * J - K
+
+    def _diis(self, F, P, S, X, fockSet, errorSet):
+        """DIIS extrapolation (mmd/scf.py:146-180); returns (F_diis, ||error||)."""
+        torch = self.context.torch
+        FPS = F @ P @ S
+        error = X @ (FPS - FPS.T) @ X
+        fockSet.append(F)
+        errorSet.append(error)
+        if len(fockSet) > 8:
+            del fockSet[0]
+            del errorSet[0]
+        n = len(fockSet)
+        E = torch.stack(errorSet).reshape(n, -1)
+        B = torch.full((n + 1, n + 1), -1.0, dtype=torch.float64, device=F.device)
+        B[:n, :n] = E @ E.T
+        B[n, n] = 0.0
+        rhs = torch.zeros(n + 1, dtype=torch.float64, device=F.device)
+        rhs[n] = -1.0
+        w = torch.linalg.solve(B, rhs)
+        Fd = torch.einsum("i,ijk->jk", w[:n], torch.stack(fockSet))
+        return Fd, float(torch.linalg.norm(error).item())
+
+    # ---------------------------------------------------------------- reference helpers
+    def orthoFock(self):
+        self.FO = np.dot(self.X.T, np.dot(self.F, self.X))
+
+    def unOrthoFock(self):
+        self.F = np.dot(self.U.T, np.dot(self.FO, self.U))
+
+    def orthoDen(self):
+        self.PO = np.dot(self.U, np.dot(self.P, self.U.T))
+
+    def unOrthoDen(self):
+        self.P = np.dot(self.X, np.dot(self.PO, self.X.T))
+
+    def computeEnergy(self):
+        self.el_energy = np.einsum("pq,qp", self.Core + self.F, self.P)
+        self.energy = self.el_energy + self.nuc_energy
+
+    def computeDipole(self):
+        self.el_energy = np.einsum("pq,qp", self.Core + self.F, self.P)
+        for i in range(3):
+            self.mu[i] = -2 * np.trace(np.dot(self.P, self.M[i])) + sum(
+                [atom.charge * (atom.origin[i] - self.center_of_charge[i]) for atom in self.atoms])
+        self.mu *= 2.541765
+
+    def adj(self, x):
+        assert x.shape[0] == x.shape[1]
+        return np.conjugate(x).T
+
+    def comm(self, A, B):
+        return np.dot(A, B) - np.dot(B, A)
+
+    def buildFock(self):
+        """Host-array Fock build from self.P / self.P_old (mmd/scf.py:82-100)."""
+        from .integrals.fock import formPT
+        if self.direct:
+            G = formPT(self.P, self.P_old, self.bfs, self.nbasis, self.screen, self.scrTol)
+            G = 0.5 * (G + G.T)
+            self.G = G
+            self.F = self.F_old + G
+        else:
+            ctx = self.context
+            torch = ctx.torch
+            Pd = torch.as_tensor(np.ascontiguousarray(np.real(self.P), dtype=np.float64), device=self._dev["S"].device)
+            Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
+            ctx.jk_dense(self._dev["TwoE"], Pd, Jd, Kd)
+            self.J = Jd.cpu().numpy()
+            self.K = Kd.cpu().numpy()
+            self.G = 2.0 * self.J - self.K
+            self.F = self.Core + self.G
+
+    def updateFock(self):
+        self.unOrthoDen()
+        self.buildFock()
+        self.orthoFock()

@@ -1,0 +1,95 @@
+"""Host-side logic (CPU): basis parsing and normalisation, shell grouping, clusters,
+flop model and the C-ABI symbol table of libmmdg.so."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_basis_normalisation_matches_oracle(golden):
+    import oracle as O
+    from mmd.integrals.twoe import Basis
+    g = golden("eri_functions.npz")
+    for o, s, k, e, c in zip(g["origin"], g["shell"], g["nprim"], g["exps"], g["coefs"]):
+        a = Basis(o, s, int(k), e[:k], c[:k])
+        b = O.Basis(o, s, int(k), e[:k], c[:k])
+        assert np.allclose(a.coefs, b.coefs, rtol=1e-14, atol=0)
+        assert np.allclose(a.norm, b.norm, rtol=1e-14, atol=0)
+
+
+def test_molecule_basis_layout(golden):
+    from mmd.molecule import Molecule
+    d = golden("mol_water_631gss.npz")
+    m = Molecule(str(d["geometry"]), "6-31gss")
+    assert m.nbasis == int(d["nbasis"]) == 25
+    assert m.nocc == 5
+    # Cartesian order of momentum2shell (mmd/molecule.py:108-114); H: s3, s1, p1
+    shells = [tuple(int(x) for x in b.shell) for b in m.bfs]
+    assert shells[-5:] == [(0, 0, 0), (0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)]
+    d_idx = [i for i, s in enumerate(shells) if sum(s) == 2]
+    assert [shells[i] for i in d_idx] == [(2, 0, 0), (1, 1, 0), (1, 0, 1), (0, 2, 0), (0, 1, 1), (0, 0, 2)]
+
+
+def test_shell_grouping():
+    from mmd.molecule import Molecule
+    from mmd.integrals.shells import shells_from_bfs
+    water = Molecule("\n0 1\nO 0 -0.075791844 0\nH 0.866811829 0.601435779 0\nH -0.866811829 0.601435779 0\n",
+                     "6-31gss")
+    ss = shells_from_bfs(water.bfs)
+    assert ss.nshell == 12
+    assert list(ss.L) == [0, 0, 1, 0, 1, 2, 0, 0, 1, 0, 0, 1]
+    # every function appears exactly once
+    f = ss.func[ss.func >= 0]
+    assert sorted(f.tolist()) == list(range(25))
+    # a ragged list: a lone d_zz, a p shell missing its y component, an s
+    bfs = [water.bfs[i] for i in (14, 2, 4, 0)]
+    ss2 = shells_from_bfs(bfs)
+    assert ss2.nshell == 3
+    assert ss2.func[0].tolist() == [-1, -1, -1, -1, -1, 0]
+    assert ss2.func[1].tolist() == [1, -1, 2, -1, -1, -1]
+
+
+def test_shell_grouping_rejects_f():
+    from mmd.integrals.twoe import Basis
+    from mmd.integrals.shells import shells_from_bfs
+    with pytest.raises(ValueError):
+        shells_from_bfs([Basis([0, 0, 0], (3, 0, 0), 1, [1.0], [1.0])])
+
+
+def test_cluster_generator():
+    from mmd.clusters import water_cluster_coords, water_cluster
+    s1, x1 = water_cluster_coords(16, seed=3)
+    s2, x2 = water_cluster_coords(16, seed=3)
+    assert np.array_equal(x1, x2) and len(s1) == 48
+    oxy = x1[0::3]
+    d = np.linalg.norm(oxy[:, None] - oxy[None], axis=-1) + np.eye(16) * 1e9
+    assert d.min() >= 2.5
+    # rigid monomers: O-H bond lengths preserved
+    for k in range(16):
+        for h in (1, 2):
+            assert abs(np.linalg.norm(x1[3 * k] - x1[3 * k + h]) - 1.0997) < 1e-3
+    assert water_cluster(2, seed=1).count("\n") == 8
+
+
+def test_flop_model():
+    from mmd.flop_model import class_flops, prim_quartet_flops
+    # (ss|ss): Boys + R only
+    assert prim_quartet_flops(0, 0, 0, 0) == 12 + 3 + 2 + 2 + 2
+    assert class_flops((1, 1, 1, 1), 1, 1, 1) > class_flops((1, 0, 0, 0), 1, 1, 1)
+
+
+def _header_symbols():
+    txt = open(os.path.join(REPO, "include", "mmdg.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(mmdg_\w+)\s*\(", txt, flags=re.M)))
+
+
+def test_capi_exports_every_declared_symbol(built_lib):
+    import ctypes
+    lib = ctypes.CDLL(built_lib)
+    syms = _header_symbols()
+    assert "mmdg_fock" in syms and "mmdg_eri_tensor" in syms and len(syms) >= 10
+    for s in syms:
+        assert hasattr(lib, s), s

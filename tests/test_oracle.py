@@ -1,0 +1,108 @@
+"""The oracle pinned against the reference's golden vectors (CPU only).
+
+* Boys function: the 48 literature values of the reference's tests/test012.py
+  (its own places=12 check plus relative 1e-9; the literature values are only
+  good to ~7e-10 relative) and an mpmath grid (relative 5e-15);
+* contracted ERIs of every angular class, the full water/STO-3G tensor and the
+  Schwarz tables: the compiled reference run in the build container;
+* formPT: the reference's own recorded calls (inputs and unsymmetrised output).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_boys_literature_values():
+    with open(os.path.join(GOLDEN, "boys_test012.json")) as f:
+        vals = json.load(f)["values"]
+    assert len(vals) == 48  # every assertAlmostEqual(boys(...)) of tests/test012.py
+    for m, T, ref in vals:
+        got = O.boys(m, T)
+        # the reference's own check: assertAlmostEqual(places=12), i.e. |diff| < 5e-13
+        assert round(got - ref, 12) == 0, (m, T, got, ref)
+        # relative: the literature values themselves carry up to 7e-10 relative error
+        # (e.g. F_25(6.4); the oracle agrees with mpmath there to 1e-15)
+        assert abs(got - ref) <= 1e-9 * abs(ref), (m, T, got, ref)
+
+
+def test_boys_mpmath_grid(golden):
+    g = golden("boys_grid.npz")
+    for im, m in enumerate(g["m"]):
+        for iT, T in enumerate(g["T"]):
+            ex = g["mpmath"][im, iT]
+            assert abs(O.boys(m, T) - ex) <= 5e-15 * abs(ex), (m, T)
+
+
+def test_boys_reference_agrees_with_mpmath(golden):
+    # the reference's own values (SciPy 1.18 hyp1f1) deviate from mpmath by up to
+    # 1e-13 relative for m <= 8 (the orders of (dd|dd)) and 3e-12 for m <= 16
+    g = golden("boys_grid.npz")
+    rel = np.abs(g["reference"] - g["mpmath"]) / np.abs(g["mpmath"])
+    assert rel[:9].max() < 2e-13
+    assert rel.max() < 5e-12
+
+
+def _functions(g):
+    bfs = []
+    for o, s, k, e, c in zip(g["origin"], g["shell"], g["nprim"], g["exps"], g["coefs"]):
+        bfs.append(O.Basis(o, s, int(k), e[:k], c[:k]))
+    return bfs
+
+
+def test_eri_every_class(golden):
+    g = golden("eri_functions.npz")
+    bfs = _functions(g)
+    q, ref = g["quartets"], g["eri"]
+    # a deterministic subset keeps the CPU suite fast (all 81 orderings covered)
+    sel = np.arange(0, len(q), 3)
+    got = np.array([O.ERI(*(bfs[i] for i in q[k])) for k in sel])
+    assert np.max(np.abs(got - ref[sel])) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["h2_sto3g", "water_sto3g", "methane_sto3g"])
+def test_eri_tensor_small(golden, name):
+    d = golden(f"mol_{name}.npz")
+    N = int(d["nbasis"])
+    T = O.doERIs(N, np.zeros((N, N, N, N)), _raw_bfs(d))
+    assert np.max(np.abs(T - d["TwoE"])) < 1e-13
+
+
+def _raw_bfs(d):
+    """Oracle Basis objects from the molecule's basis file (raw contraction coefficients)."""
+    from mmd.molecule import Molecule
+    m = Molecule(str(d["geometry"]), str(d["basis"]))
+    out = []
+    for atom in m.atoms:
+        for momentum, prims in m.basis_data[atom.charge]:
+            exps = [e for e, c in prims]
+            coefs = [c for e, c in prims]
+            for shell in m.momentum2shell(momentum):
+                out.append(O.Basis(atom.origin, shell, len(exps), exps, coefs))
+    return out
+
+
+@pytest.mark.parametrize("name", ["water_sto3g", "methane_sto3g", "water_631g", "helium_ccpvtz"])
+def test_screen_table(golden, name):
+    d = golden(f"mol_{name}.npz")
+    scr = O.screen_table(_raw_bfs(d))
+    assert np.max(np.abs(scr - d["screen"])) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["h2_sto3g", "water_sto3g", "methane_sto3g", "water_631g"])
+def test_formPT_records(golden, name):
+    d = golden(f"mol_{name}.npz")
+    bfs = _raw_bfs(d)
+    N = int(d["nbasis"])
+    k = 0
+    while f"formPT{k}_G" in d:
+        assert np.all(d[f"formPT{k}_imag"] == 0.0)
+        G = O.formPT(d[f"formPT{k}_P"], d[f"formPT{k}_Pold"], bfs, N, d["screen"], 1e-12)
+        assert np.max(np.abs(G.real - d[f"formPT{k}_G"])) < 1e-13
+        k += 1
+    assert k >= 1
