@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark of the two-electron hot path: direct RHF on a seeded (H2O)16 cluster.
+
+Workload (the reference metric's single-GPU configuration): 16 water monomers on a
+4x4x1 lattice at 3.0 Angstrom, rigidly rotated (uniform quaternions) and jittered
+(+-0.3 Angstrom), seed 16; basis 6-31G** with Cartesian d (400 functions, 192
+shells); direct SCF with Schwarz x density screening at 1e-12 (formPT semantics,
+incremental Fock builds); FP64.  Synthetic data: the geometry is generated, no
+dataset is involved.
+
+One *step* is one RHF iteration with a Fock build (G(P - P_old) on the GPU,
+symmetrised incremental update, DIIS, eigensolve, density, energy).  W warm-up
+iterations run on a first SCF; the K timed steps are iterations 1..K of a fresh SCF
+from the core guess (iteration 0 only diagonalises the core Hamiltonian).
+Between timed steps a 512 MB buffer is written to flush the 129 MB L2.
+
+Printed (rank 0, one JSON line):
+  value      Fock builds/s (= RHF iterations/s), device-timed with CUDA events
+  e2e        the same metric through the reference-facing API formPT(P, P_old,
+             bfs, nbasis, screen, tol) with host arrays in and out
+  time_to_converge_s  Molecule(geometry, basis).RHF(direct=True) wall time (conver 1e-8)
+  roofline   FP64-pipe roofline of the dominant class kernel (live CUDA events,
+             model FLOPs of mmd/flop_model.py, peak measured live by mmdg_measure_peaks)
+  cpu_baseline  the reference's Cython formPT (oracle/_ref) on the host cores, a
+             bounded sample extrapolated to this workload (see cpu_sample())
+
+``--impl reference`` times the reference's CPU implementation alone (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "mcmurchie-davidson_gb300")
+ORACLE = os.path.join(REPO, "oracle")
+
+WORKLOAD = {"workload": "(H2O)16 6-31G** direct RHF", "n_water": 16, "lattice": "4x4x1", "spacing_A": 3.0,
+            "jitter_A": 0.3, "seed": 16, "basis": "6-31G**", "nbasis": 400, "schwarz": 1e-12}
+# Average number of function quartets that pass the reference's screening per Fock
+# build over iterations 1..20 of the workload above (the GPU arm counts them with
+# the same rule and prints its own figure as config.fq_per_build).  Used by the
+# reference arm, which cannot run the 400-function SCF itself.
+FQ_PER_BUILD = None
+
+
+def _env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names[1:], p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------ CPU sample
+def _ref_worker_init(spec_path):
+    global _W
+    with open(spec_path) as f:
+        spec = json.load(f)
+    import numpy as np
+    kind = spec["kind"]
+    if kind == "reference":
+        sys.path.insert(0, os.path.join(ORACLE, "_ref"))
+        from mmd.integrals.twoe import Basis
+        from mmd.integrals.fock import formPT
+        bfs = [Basis(np.array(o), np.array(s), len(e), np.array(e), np.array(c)) for o, s, e, c in spec["bfs"]]
+        screen = {i: v for i, v in enumerate(spec["screen"])}
+    else:
+        sys.path.insert(0, ORACLE)
+        import oracle as O
+        bfs = [O.Basis(o, s, len(e), e, c) for o, s, e, c in spec["bfs"]]
+        formPT = O.formPT
+        screen = np.array(spec["screen"])
+    P = np.array(spec["P"], dtype=complex)
+    _W = (formPT, bfs, screen, P, len(bfs))
+
+
+def _ref_worker_run(mode):
+    import numpy as np
+    formPT, bfs, screen, P, N = _W
+    Pold = P if mode == "skip" else np.zeros_like(P)
+    t0 = time.perf_counter()
+    formPT(P, Pold, bfs, N, screen, 1e-12)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(spec_path, cores, steps, warmup):
+    """Time the reference formPT on water/6-31G** in `cores` processes.
+
+    Two calls per process and step: dP = 0 (every candidate quartet is screened
+    out: the per-candidate screening cost of formPT's Python loop) and dP = P1 (the
+    reference's first-iteration density: nearly every quartet survives).  The
+    per-build time of the target is then  n_cand * t_skip + n_surv * t_eri  with
+    t_eri = (t_full - t_skip) / n_surv_monomer.  Prints one JSON object."""
+    import multiprocessing as mp
+    with open(spec_path) as f:
+        spec = json.load(f)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_ref_worker_init, initargs=(spec_path,)) as pool:
+        for _ in range(max(warmup, 1)):
+            pool.map(_ref_worker_run, ["skip"] * cores)
+        t_skip, t_full = [], []
+        for _ in range(steps):
+            t_skip.append(max(pool.map(_ref_worker_run, ["skip"] * cores)))
+            t_full.append(max(pool.map(_ref_worker_run, ["full"] * cores)))
+    ts, tf = sum(t_skip) / len(t_skip), sum(t_full) / len(t_full)
+    n_cand_m, n_surv_m = spec["n_cand_monomer"], spec["n_surv_monomer"]
+    t_cand = ts / n_cand_m
+    t_eri = max(tf - ts, 1e-12) / n_surv_m
+    t_build = spec["n_cand_target"] * t_cand + spec["n_surv_target"] * t_eri
+    out = {"kind": spec["kind"], "cores": cores, "t_skip_s": ts, "t_full_s": tf, "t_candidate_s": t_cand,
+           "t_eri_s": t_eri, "t_build_1core_s": t_build, "builds_per_s": cores / t_build,
+           "quartets_per_s_1core": 1.0 / t_eri, "steps": steps}
+    print(json.dumps(out))
+
+
+def _monomer_spec(kind):
+    """Basis (raw coefficients), Schwarz table and first-iteration density of water/6-31G**
+    for the CPU sample; all from the repository (tests/golden holds the reference's own run)."""
+    import numpy as np
+    sys.path.insert(0, PKG)
+    from mmd.molecule import Molecule
+    g = np.load(os.path.join(REPO, "tests", "golden", "mol_water_631gss.npz"))
+    m = Molecule(str(g["geometry"]), "6-31gss")
+    bfs = []
+    for atom in m.atoms:
+        for momentum, prims in m.basis_data[atom.charge]:
+            ex = [e for e, c in prims]
+            co = [c for e, c in prims]
+            for sh in m.momentum2shell(momentum):
+                bfs.append((list(map(float, atom.origin)), list(sh), ex, co))
+    N = len(bfs)
+    P1 = g["formPT0_P"]
+    scr = g["screen"]
+    # survivors of the reference's screening rule for dP = P1 (fock.pyx:46-57)
+    sq = np.sqrt(scr)
+    iu = np.array([(i, j) for i in range(N) for j in range(i + 1)])
+    d = np.abs(P1)
+    n_surv = 0
+    for a in range(len(iu)):
+        i, j = iu[a]
+        kl = iu[: a + 1]
+        k, l = kl[:, 0], kl[:, 1]
+        dm = np.maximum.reduce([np.full(len(kl), 4 * d[i, j]), 4 * d[k, l], d[i, k], d[i, l], d[j, k], d[j, l]])
+        n_surv += int(np.sum(sq[a] * sq[: a + 1] * dm >= 1e-12))
+    npair = N * (N + 1) // 2
+    return {"kind": kind, "bfs": bfs, "screen": scr.tolist(), "P": P1.tolist(),
+            "n_cand_monomer": npair * (npair + 1) // 2, "n_surv_monomer": n_surv}
+
+
+def run_cpu_sample(n_cand_target, n_surv_target, steps, warmup, cores=None):
+    kind = "reference" if os.path.isdir(os.path.join(ORACLE, "_ref", "mmd", "integrals")) and any(
+        f.startswith("fock") and f.endswith(".so") for f in os.listdir(os.path.join(ORACLE, "_ref", "mmd", "integrals"))
+    ) else "port"
+    if kind == "port":
+        subprocess.check_call(["make", "-s", "-C", ORACLE, "liboracle.so"])
+    spec = _monomer_spec(kind)
+    spec["n_cand_target"] = n_cand_target
+    spec["n_surv_target"] = n_surv_target
+    cores = cores or os.cpu_count()
+    with tempfile.NamedTemporaryFile("w", suffix=".json", delete=False) as f:
+        json.dump(spec, f)
+        path = f.name
+    try:
+        out = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", path, "--cores", str(cores),
+                              "--steps", str(steps), "--warmup", str(warmup)],
+                             capture_output=True, text=True, check=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    finally:
+        os.unlink(path)
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    res["sample"] = (f"reference formPT on water/6-31G** (N=25, {spec['n_cand_monomer']} candidate and "
+                     f"{spec['n_surv_monomer']} surviving quartets) in {cores} processes, dP=0 and dP=P1 per step; "
+                     f"extrapolated to {n_cand_target:.4g} candidates and {n_surv_target:.4g} survivors per build")
+    return res
+
+
+# ------------------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import numpy as np
+    import torch
+    rank, world, local = _env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sys.path.insert(0, PKG)
+    from mmd import _native, flop_model
+    from mmd.clusters import water_cluster
+    from mmd.integrals.fock import formPT
+    from mmd.molecule import Molecule
+
+    geom = water_cluster(WORKLOAD["n_water"], seed=WORKLOAD["seed"])
+    fp32 = args.fp32_below
+    # ---------------- warm-up SCF
+    mol = Molecule(geom, "6-31gss")
+    N = mol.nbasis
+    st = mol.scf_begin(direct=True, acc2e=WORKLOAD["schwarz"], fp32_below=fp32)
+    for _ in range(args.warmup + 1):
+        st.iterate()
+    # ---------------- timed: iterations 1..K of a fresh SCF
+    st = mol.scf_begin(direct=True, acc2e=WORKLOAD["schwarz"], fp32_below=fp32, build=False)
+    st.iterate()  # iteration 0: core-Hamiltonian diagonalisation, no Fock build
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float64, device="cuda")
+    mol._fock_profile = {}
+    dens = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record()
+        st.iterate()
+        ev[k][1].record()
+        dens.append(st.last_dP)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    prof = mol._fock_profile
+    mol._fock_profile = None
+    t_dev = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    builds = args.steps
+    value = world * builds / t_dev
+    counts = prof["counts"].reshape(-1, 3)
+    class_ms = prof["class_ms"]
+    fq_per_build = float(counts[:, 0].sum()) / builds
+    # ---------------- roofline of the dominant class kernel
+    ctx = mol.context
+    fp64_peak, fp32_peak = _native.measure_peaks(ctx)
+    cls_flops = np.array([flop_model.class_flops(c, row[2], row[0]) for c, row in zip(flop_model.CLASSES, counts)])
+    cls_exec = np.array([flop_model.executed_flops_per_prim_quartet(*c) * row[2] + 12.0 * row[0]
+                         for c, row in zip(flop_model.CLASSES, counts)])
+    dom = int(np.argmax(class_ms))
+    dom_cls = flop_model.CLASSES[dom]
+    achieved = cls_flops[dom] / (class_ms[dom] / 1e3) / 1e12
+    build_ms = float(class_ms.sum()) / builds
+    all_achieved = float(cls_flops.sum()) / (float(class_ms.sum()) / 1e3) / 1e12
+    roofline = {"bound": "fp64", "kernel": "k_fock<MD_%d%d%d%d,double>" % dom_cls, "achieved": achieved,
+                "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "live DFMA probe mmdg_measure_peaks (MEASURED_PEAKS.json has no FP64 figure)",
+                "flops_per_launch": float(cls_flops[dom]) / builds, "launch_ms": float(class_ms[dom]) / builds,
+                "all_classes": {"achieved": all_achieved, "frac": all_achieved / fp64_peak,
+                                "fock_build_ms": build_ms,
+                                "executed_achieved": float(cls_exec.sum()) / (float(class_ms.sum()) / 1e3) / 1e12},
+                "fp32_peak": fp32_peak}
+    # ---------------- e2e through formPT with host arrays
+    Ph = [(a.cpu().numpy(), b.cpu().numpy()) for a, b in dens]
+    screen = mol.screen
+    formPT(Ph[0][0], Ph[0][1], mol.bfs, N, screen, WORKLOAD["schwarz"])  # context / screen already cached
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for P, Po in Ph:
+        G = formPT(P, Po, mol.bfs, N, screen, WORKLOAD["schwarz"])
+    t_e2e = time.perf_counter() - t0
+    del G
+    e2e = {"value": world * len(Ph) / t_e2e, "unit": "Fock builds/s", "api": "mmd.integrals.fock.formPT (host arrays)",
+           "h2d_bytes_per_step": N * N * 8, "d2h_bytes_per_step": N * N * 8}
+    # ---------------- time to converge through Molecule(...).RHF (fresh device context)
+    ttc, E, iters = None, None, None
+    if not args.no_ttc:
+        from mmd.integrals import twoe
+        twoe._ctx_cache.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m2 = Molecule(geom, "6-31gss")
+        E = float(m2.RHF(doPrint=False, direct=True, fp32_below=fp32))
+        ttc = time.perf_counter() - t0
+        iters = int(m2.iterations)
+    # ---------------- CPU baseline (rank 0, N = 1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        npair = N * (N + 1) // 2
+        try:
+            cb = run_cpu_sample(npair * (npair + 1) // 2, fq_per_build, steps=2, warmup=1)
+            cpu = {"value": cb["builds_per_s"], "unit": "Fock builds/s", "cores": cb["cores"], "kind": cb["kind"],
+                   "sample": cb["sample"], "t_build_1core_s": cb["t_build_1core_s"],
+                   "quartets_per_s_1core": cb["quartets_per_s_1core"]}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "error": str(e)[:300]}
+    # our kernels per Fock build: |dP| copy, shell-block maxima, one launch per class
+    # (two with the FP32 split), symmetrised update
+    launches_per_build = 3 + len(flop_model.CLASSES) * (2 if fp32 > 0 else 1)
+    line = {
+        "metric": "Fock builds/s ((H2O)16 6-31G** direct RHF, 20 iterations)",
+        "value": value, "unit": "Fock builds/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / builds, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if fp32 == 0 else "f64+f32", "data": "synthetic (seeded cluster geometry)",
+        "config": dict(WORKLOAD, fp32_below=fp32, l2="flushed between steps (512 MB write)",
+                       fq_per_build=fq_per_build, eris_per_s=fq_per_build * value / world,
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "e2e": e2e, "time_to_converge_s": ttc, "scf_iterations": iters, "energy": E,
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "gpu_launches": launches_per_build * builds, "wall_s": wall,
+        "class_ms_per_build": {"%d%d%d%d" % c: float(x) / builds for c, x in zip(flop_model.CLASSES, class_ms)},
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------ reference arm
+def reference_arm(args):
+    rank, world, _ = _env()
+    if rank != 0:
+        return
+    npair = 400 * 401 // 2
+    if FQ_PER_BUILD is None:
+        print(json.dumps({"impl": "reference", "unavailable": "survivor count of the workload not yet recorded"}))
+        return
+    cb = run_cpu_sample(npair * (npair + 1) // 2, FQ_PER_BUILD, steps=args.steps, warmup=args.warmup)
+    v = cb["builds_per_s"]
+    line = {"impl": "reference", "metric": "Fock builds/s ((H2O)16 6-31G** direct RHF, 20 iterations)", "value": v,
+            "unit": "Fock builds/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded cluster geometry)", "config": dict(WORKLOAD),
+            "cpu_baseline": {"value": v, "unit": "Fock builds/s", "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp32-below", type=float, default=0.0, help="Schwarz bound below which quartets run in FP32")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge run")
+    ap.add_argument("--cpu-sample", metavar="SPEC")
+    ap.add_argument("--cores", type=int, default=None)
+    args = ap.parse_args()
+    if args.cpu_sample:
+        cpu_sample(args.cpu_sample, args.cores or os.cpu_count(), args.steps, args.warmup)
+    elif args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -104,6 +104,17 @@ int mmdg_eri_tensor(mmdg_context* ctx, double* out, void* stream);
 int mmdg_fock(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below,
               unsigned long long* counts, void* stream);
 
+/* mmdg_fock with CUDA events around every class launch: class_ms[MMDG_NCLASS]
+ * receives each class's device time in ms (synchronises the stream).  Measurement
+ * support; no counterpart in the reference. */
+int mmdg_fock_timed(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below,
+                    unsigned long long* counts, float* class_ms, void* stream);
+
+/* FP64 (DFMA) and FP32 (FFMA) throughput of this GPU in TFLOP/s, from independent
+ * FMA chains on every SM: the roofline denominators of the ERI kernels.
+ * Measurement support; no counterpart in the reference. */
+int mmdg_measure_peaks(mmdg_context* ctx, double* fp64_tflops, double* fp32_tflops);
+
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
 

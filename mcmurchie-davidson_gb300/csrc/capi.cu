@@ -594,8 +594,22 @@ __global__ void k_shell_dmax(const float* dPf, float* Dsh, const int* func, cons
   Dsh[mol_sbase[m] + (long long)sh_local[s1] * S + sh_local[s2]] = mx;
 }
 
+static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
+                     unsigned long long* counts, float* class_ms, void* stream);
+
 extern "C" int mmdg_fock(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
                          unsigned long long* counts, void* stream) {
+  return fock_impl(h, dP, G, tol, fp32_below, counts, nullptr, stream);
+}
+
+extern "C" int mmdg_fock_timed(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
+                               unsigned long long* counts, float* class_ms, void* stream) {
+  if (!class_ms) return fail(MMDG_E_ARG, "mmdg_fock_timed: null class_ms");
+  return fock_impl(h, dP, G, tol, fp32_below, counts, class_ms, stream);
+}
+
+static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
+                     unsigned long long* counts, float* class_ms, void* stream) {
   if (!h || !dP || !G) return fail(MMDG_E_ARG, "mmdg_fock: null argument");
   if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_fock: no basis set");
   if (!(tol >= 0.0) || !(fp32_below >= 0.0)) return fail(MMDG_E_ARG, "mmdg_fock: negative threshold");
@@ -625,19 +639,30 @@ extern "C" int mmdg_fock(mmdg_context* h, const double* dP, double* G, double to
   f.tolf_lo = float(tol * (1.0 - 1e-4));
   f.tolf_hi = float(tol * (1.0 + 1e-4));
   const float split = float(fp32_below);
+  cudaEvent_t ev[2 * MMDG_NCLASS];
+  if (class_ms)
+    for (int k = 0; k < 2 * MMDG_NCLASS; ++k) CUDA_TRY(cudaEventCreate(&ev[k]));
   int ci = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     f.counters = h->d_counters.p + 3 * ci;
-    ++ci;
-    if (!h->cls_count[cb] || !h->cls_count[ck]) continue;
-    ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, split, INFINITY};
-    CUDA_TRY(e.fock(0, g, f, cl, st));
-    if (split > 0.f) {
-      cl.qmin = 0.f;
-      cl.qmax = split;
-      CUDA_TRY(e.fock(1, g, f, cl, st));
+    if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
+    if (h->cls_count[cb] && h->cls_count[ck]) {
+      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, split, INFINITY};
+      CUDA_TRY(e.fock(0, g, f, cl, st));
+      if (split > 0.f) {
+        cl.qmin = 0.f;
+        cl.qmax = split;
+        CUDA_TRY(e.fock(1, g, f, cl, st));
+      }
     }
+    if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
+    ++ci;
+  }
+  if (class_ms) {
+    CUDA_TRY(cudaEventSynchronize(ev[2 * MMDG_NCLASS - 1]));
+    for (int k = 0; k < MMDG_NCLASS; ++k) CUDA_TRY(cudaEventElapsedTime(&class_ms[k], ev[2 * k], ev[2 * k + 1]));
+    for (int k = 0; k < 2 * MMDG_NCLASS; ++k) cudaEventDestroy(ev[k]);
   }
   if (counts) {
     CUDA_TRY(cudaMemcpyAsync(counts, h->d_counters.p, sizeof(unsigned long long) * 3 * MMDG_NCLASS,
@@ -1034,5 +1059,55 @@ extern "C" int mmdg_one_electron(mmdg_context* h, int natom, const int* atom_mol
   k_one_electron<<<(h->npair + 63) / 64, 64, 0, st>>>(a);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(st));  // the temporary atom buffers are freed on return
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ peak probe
+// Throughput of dependent-free FMA chains: the FP64 (DFMA) and FP32 (FFMA) roofline
+// denominators of this GPU, measured at the clocks of the moment.
+template <typename T>
+__global__ void k_fma_probe(T* out, int iters, T a, T b) {
+  T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+      x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int mmdg_measure_peaks(mmdg_context* h, double* fp64_tflops, double* fp32_tflops) {
+  if (!h || !fp64_tflops || !fp32_tflops) return fail(MMDG_E_ARG, "mmdg_measure_peaks: null argument");
+  DeviceGuard dg(h->device);
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  const int blocks = sms * 8, threads = 256;
+  DevBuf<double> out;
+  if (out.alloc((size_t)blocks * threads)) return fail(MMDG_E_NOMEM, "mmdg_measure_peaks: allocation");
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  float ms = 0.f;
+  const double n = double(blocks) * threads;
+  k_fma_probe<double><<<blocks, threads>>>(out.p, 20, 0.999, 1e-3);
+  CUDA_TRY(cudaEventRecord(e0));
+  k_fma_probe<double><<<blocks, threads>>>(out.p, 400, 0.999, 1e-3);
+  CUDA_TRY(cudaEventRecord(e1));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+  *fp64_tflops = 2.0 * 64 * 400 * n / (ms * 1e-3) / 1e12;
+  float* fo = reinterpret_cast<float*>(out.p);
+  k_fma_probe<float><<<blocks, threads>>>(fo, 200, 0.999f, 1e-3f);
+  CUDA_TRY(cudaEventRecord(e0));
+  k_fma_probe<float><<<blocks, threads>>>(fo, 20000, 0.999f, 1e-3f);
+  CUDA_TRY(cudaEventRecord(e1));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+  *fp32_tflops = 2.0 * 64 * 20000 * n / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CUDA_TRY(cudaGetLastError());
   return MMDG_OK;
 }

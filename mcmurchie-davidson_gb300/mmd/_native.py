@@ -37,6 +37,8 @@ def _bind(L):
         "mmdg_set_screen": (c_int, [p, p, c_ll]),
         "mmdg_eri_tensor": (c_int, [p, p, p]),
         "mmdg_fock": (c_int, [p, p, p, c_d, c_d, p, p]),
+        "mmdg_fock_timed": (c_int, [p, p, p, c_d, c_d, p, p, p]),
+        "mmdg_measure_peaks": (c_int, [p, p, p]),
         "mmdg_boys": (c_int, [p, c_int, c_ll, p, p, p]),
         "mmdg_fock_update": (c_int, [p, p, p, p, p]),
         "mmdg_jk_dense": (c_int, [p, c_ll, p, p, p, p, p]),
@@ -167,6 +169,18 @@ class Context:
             self.last_counts = cnt.reshape(NCLASS, 3)
         return G
 
+    def fock_timed(self, dP, G=None, tol: float = 1e-12, fp32_below: float = 0.0):
+        """As ``fock`` with per-class device times (ms) and counts: returns (G, class_ms, counts)."""
+        if G is None:
+            G = self.torch.empty_like(dP)
+        cnt = np.zeros(3 * NCLASS, dtype=np.uint64)
+        ms = np.zeros(NCLASS, dtype=np.float32)
+        check(lib().mmdg_fock_timed(self._h, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(G.data_ptr()),
+                                    float(tol), float(fp32_below), _ptr(cnt), _ptr(ms), stream_ptr()),
+              "mmdg_fock_timed")
+        self.last_counts = cnt.reshape(NCLASS, 3)
+        return G, ms, self.last_counts
+
     def fock_update(self, G, F_in, F_out):
         check(lib().mmdg_fock_update(self._h, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(F_in.data_ptr()),
                                      ctypes.c_void_p(F_out.data_ptr()), stream_ptr()), "mmdg_fock_update")
@@ -184,6 +198,14 @@ class Context:
         check(lib().mmdg_boys(self._h, int(m), T.numel(), ctypes.c_void_p(T.data_ptr()),
                               ctypes.c_void_p(out.data_ptr()), stream_ptr()), "mmdg_boys")
         return out
+
+
+def measure_peaks(ctx) -> tuple[float, float]:
+    """(FP64, FP32) TFLOP/s of the current GPU (independent FMA chains)."""
+    a = ctypes.c_double()
+    b = ctypes.c_double()
+    check(lib().mmdg_measure_peaks(ctx._h, ctypes.byref(a), ctypes.byref(b)), "mmdg_measure_peaks")
+    return a.value, b.value
 
 
 _default_ctx = None

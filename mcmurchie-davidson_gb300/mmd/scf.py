@@ -33,96 +33,21 @@ class SCF(object):
     """SCF methods for the molecule object (mmd/scf.py:8-180)."""
 
     def RHF(self, doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12, fp32_below=0.0, guess=None,
-            guess_fallback=True, maxiter=100, _timings=None):
-        self.is_converged = False
-        self.delta_energy = 1e20
-        self.P_RMS = 1e20
-        self.maxiter = int(maxiter)
-        self.direct = direct
-        if self.direct:
-            self.incFockRst = False
-        self.scrTol = acc2e
-        self.fp32_below = float(fp32_below)
-        self.build(self.direct)
-        ctx = self.context
-        torch = ctx.torch
-        N = self.nbasis
-        dev = self._dev["S"].device
-        dd = self._dev
-        Core, X, S = dd["Core"], dd["X"], dd["S"]
-        if not self.direct:
-            self._TwoE_dev = dd["TwoE"]
-        self.fock_builds = 0
-        self.fock_time = 0.0
-        self.guess_used = guess is not None
-        self.guess_reverted = False
-
-        P_old = torch.zeros((N, N), dtype=torch.float64, device=dev)
-        P = P_old
-        F = Core.clone()
-        if guess is not None:
-            Pg = torch.as_tensor(np.asarray(guess, dtype=np.float64), device=dev)
-            G = self._two_electron(Pg, torch.zeros_like(Pg))
-            F = Core + G
-            P_old = Pg
-            P = Pg
-        fockSet, errorSet = [], []
-        energy = None
-        FO = None
-        err_hist = []
+            guess_fallback=True, maxiter=100):
+        state = self.scf_begin(DIIS=DIIS, direct=direct, acc2e=acc2e, fp32_below=fp32_below, guess=guess,
+                               guess_fallback=guess_fallback, maxiter=maxiter)
         t_start = time.perf_counter()
         for step in range(self.maxiter):
-            if step > 0:
-                F_old = F
-                energy_old = energy
-                if self.direct:
-                    G = self._two_electron(P, P_old)
-                    F = torch.empty_like(F_old)
-                    ctx.fock_update(G, F_old, F)
-                else:
-                    F = self._conventional_fock(P)
-                P_old = P
-                if DIIS:
-                    F_diis, derr = self._diis(F, P, S, X, fockSet, errorSet)
-                    FO = X.T @ F_diis @ X
-                    err_hist.append(derr)
-                    if (self.guess_used and guess_fallback and not self.guess_reverted and len(err_hist) >= 4
-                            and err_hist[-1] > err_hist[-2] > err_hist[-3] > err_hist[-4]):
-                        # learned/initial guess misbehaves: restart from the core guess
-                        self.guess_reverted = True
-                        P_old = torch.zeros_like(P)
-                        F = Core.clone()
-                        fockSet.clear()
-                        errorSet.clear()
-                        FO = X.T @ F @ X
-            if not DIIS or step == 0:
-                FO = X.T @ F @ X
-            E, CO = torch.linalg.eigh(FO)
-            C = X @ CO
-            Cocc = C[:, : self.nocc]
-            P = Cocc @ Cocc.T
-            energy = float(torch.sum((Core + F) * P.T).item()) + self.nuc_energy
-            if step > 0:
-                self.delta_energy = energy - energy_old
-                self.P_RMS = float(torch.linalg.norm(P - P_old).item())
+            state.iterate()
             if np.abs(self.P_RMS) < conver or step == (self.maxiter - 1):
                 if step == (self.maxiter - 1):
                     print("NOT CONVERGED")
                 else:
                     self.is_converged = True
-                self.iterations = step
                 break
+        self.iterations = step
         self.scf_time = time.perf_counter() - t_start
-        # results back to the reference's attribute names (host arrays)
-        self.P = P.cpu().numpy()
-        self.P_old = P_old.cpu().numpy()
-        self.F = F.cpu().numpy()
-        self.FO = FO.cpu().numpy()
-        self.C = C.cpu().numpy()
-        self.CO = CO.cpu().numpy()
-        self.MO = E.cpu().numpy()
-        self.energy = np.float64(energy)
-        self.el_energy = self.energy - self.nuc_energy
+        state.finish()
         if self.is_converged:
             FPS = self.F @ self.P @ self.S
             error = FPS - FPS.T
@@ -138,13 +63,36 @@ class SCF(object):
                 print("  Dipole Z = ", "{0:.8f}".format(self.mu[2].real))
         return self.energy
 
+    def scf_begin(self, DIIS=True, direct=False, acc2e=1e-12, fp32_below=0.0, guess=None, guess_fallback=True,
+                  maxiter=100, build=True):
+        """Integrals and the initial state of an RHF run; returns the iteration object."""
+        self.is_converged = False
+        self.delta_energy = 1e20
+        self.P_RMS = 1e20
+        self.maxiter = int(maxiter)
+        self.direct = direct
+        if self.direct:
+            self.incFockRst = False
+        self.scrTol = acc2e
+        self.fp32_below = float(fp32_below)
+        if build or not getattr(self, "is_built", False):
+            self.build(self.direct)
+        return _RHFState(self, DIIS, guess, guess_fallback)
+
     # ---------------------------------------------------------------- pieces
     def _two_electron(self, P, P_old):
         """Unsymmetrised G(P - P_old) on the GPU, symmetrised: (G + G^T)/2."""
         ctx = self.context
         t0 = time.perf_counter()
         dP = (P - P_old).contiguous().view(-1)
-        G = ctx.fock(dP, tol=self.scrTol, fp32_below=self.fp32_below)
+        prof = getattr(self, "_fock_profile", None)
+        if prof is not None:  # per-class device times and counts (measurement)
+            G, ms, cnt = ctx.fock_timed(dP, tol=self.scrTol, fp32_below=self.fp32_below)
+            prof["class_ms"] = prof.get("class_ms", 0.0) + ms.astype(np.float64)
+            prof["counts"] = prof.get("counts", 0) + cnt.astype(np.float64)
+            prof["builds"] = prof.get("builds", 0) + 1
+        else:
+            G = ctx.fock(dP, tol=self.scrTol, fp32_below=self.fp32_below)
         self.fock_builds += 1
         self.fock_time += time.perf_counter() - t0
         G = G.view(self.nbasis, self.nbasis)
@@ -234,3 +182,94 @@ class SCF(object):
         self.unOrthoDen()
         self.buildFock()
         self.orthoFock()
+
+
+class _RHFState:
+    """One RHF run on the device; ``iterate()`` is one pass of mmd/scf.py:30-60."""
+
+    def __init__(self, mol, DIIS, guess, guess_fallback):
+        self.mol = mol
+        ctx = mol.context
+        self.ctx = ctx
+        torch = ctx.torch
+        self.torch = torch
+        dd = mol._dev
+        self.Core, self.X, self.S = dd["Core"], dd["X"], dd["S"]
+        if not mol.direct:
+            mol._TwoE_dev = dd["TwoE"]
+        self.DIIS = DIIS
+        self.guess_fallback = guess_fallback
+        mol.fock_builds = 0
+        mol.fock_time = 0.0
+        mol.guess_used = guess is not None
+        mol.guess_reverted = False
+        N = mol.nbasis
+        self.P_old = torch.zeros((N, N), dtype=torch.float64, device=self.S.device)
+        self.P = self.P_old
+        self.F = self.Core.clone()
+        if guess is not None:
+            Pg = torch.as_tensor(np.asarray(guess, dtype=np.float64), device=self.S.device)
+            self.F = self.Core + mol._two_electron(Pg, torch.zeros_like(Pg))
+            self.P_old = Pg
+            self.P = Pg
+        self.fockSet, self.errorSet, self.err_hist = [], [], []
+        self.energy = None
+        self.FO = None
+        self.step = 0
+        self.last_dP = None
+
+    def iterate(self):
+        mol, torch = self.mol, self.torch
+        X, S, Core = self.X, self.S, self.Core
+        if self.step > 0:
+            F_old = self.F
+            energy_old = self.energy
+            if mol.direct:
+                self.last_dP = (self.P, self.P_old)
+                G = mol._two_electron(self.P, self.P_old)
+                F = torch.empty_like(F_old)
+                mol.context.fock_update(G, F_old, F)
+                self.F = F
+            else:
+                self.F = mol._conventional_fock(self.P)
+            self.P_old = self.P
+            if self.DIIS:
+                F_diis, derr = mol._diis(self.F, self.P, S, X, self.fockSet, self.errorSet)
+                self.FO = X.T @ F_diis @ X
+                eh = self.err_hist
+                eh.append(derr)
+                if (mol.guess_used and self.guess_fallback and not mol.guess_reverted and len(eh) >= 4
+                        and eh[-1] > eh[-2] > eh[-3] > eh[-4]):
+                    # the initial guess misbehaves: restart from the core guess
+                    mol.guess_reverted = True
+                    self.P_old = torch.zeros_like(self.P)
+                    self.F = Core.clone()
+                    self.fockSet.clear()
+                    self.errorSet.clear()
+                    self.FO = X.T @ self.F @ X
+        if not self.DIIS or self.step == 0:
+            self.FO = X.T @ self.F @ X
+        E, CO = torch.linalg.eigh(self.FO)
+        self.E, self.CO = E, CO
+        self.C = X @ CO
+        Cocc = self.C[:, : mol.nocc]
+        self.P = Cocc @ Cocc.T
+        self.energy = float(torch.sum((Core + self.F) * self.P.T).item()) + mol.nuc_energy
+        if self.step > 0:
+            mol.delta_energy = self.energy - energy_old
+            mol.P_RMS = float(torch.linalg.norm(self.P - self.P_old).item())
+        mol.energy = np.float64(self.energy)
+        self.step += 1
+
+    def finish(self):
+        """Results back to the reference's attribute names (host arrays)."""
+        mol = self.mol
+        mol.P = self.P.cpu().numpy()
+        mol.P_old = self.P_old.cpu().numpy()
+        mol.F = self.F.cpu().numpy()
+        mol.FO = self.FO.cpu().numpy()
+        mol.C = self.C.cpu().numpy()
+        mol.CO = self.CO.cpu().numpy()
+        mol.MO = self.E.cpu().numpy()
+        mol.energy = np.float64(self.energy)
+        mol.el_energy = mol.energy - mol.nuc_energy

@@ -144,11 +144,14 @@ def test_formPT_vs_oracle_random_density():
 
 @pytest.mark.parametrize("name", MOLS)
 def test_rhf_energy_conventional(name):
+    """Tightly converged (conver 1e-12, dE < 1e-10) energies agree to 1e-10 Eh.  At the
+    default conver = 1e-8 the stopping iterate is path dependent (rounding in eigh and
+    DIIS moves it by ~1e-9), so that energy is held to the convergence scale, 1e-8."""
     d = _load(f"mol_{name}.npz")
-    E = _mol(d).RHF(doPrint=False)
-    assert abs(E - float(d["energy_conv"])) < 1e-10, (E, float(d["energy_conv"]))
     E12 = _mol(d).RHF(doPrint=False, conver=1e-12)
-    assert abs(E12 - float(d["energy_conv_1e12"])) < 1e-10
+    assert abs(E12 - float(d["energy_conv_1e12"])) < 1e-10, (E12, float(d["energy_conv_1e12"]))
+    E = _mol(d).RHF(doPrint=False)
+    assert abs(E - float(d["energy_conv"])) < 1e-8, (E, float(d["energy_conv"]))
 
 
 @pytest.mark.parametrize("name", [m for m in MOLS if "energy_direct" in _load(f"mol_{m}.npz")])
@@ -156,8 +159,11 @@ def test_rhf_energy_direct(name):
     d = _load(f"mol_{name}.npz")
     mol = _mol(d)
     E = mol.RHF(doPrint=False, direct=True)
-    assert abs(E - float(d["energy_direct"])) < 1e-10, (E, float(d["energy_direct"]))
+    assert abs(E - float(d["energy_direct"])) < 1e-8, (E, float(d["energy_direct"]))
     assert mol.is_converged
+    # tightly converged direct SCF equals the tightly converged conventional reference
+    E12 = _mol(d).RHF(doPrint=False, direct=True, conver=1e-12)
+    assert abs(E12 - float(d["energy_conv_1e12"])) < 1e-10, (E12, float(d["energy_conv_1e12"]))
 
 
 def test_dipole_water():
