@@ -243,6 +243,8 @@ def gpu_arm(args):
     from mmd.integrals.fock import formPT
     from mmd.molecule import Molecule
 
+    if args.n_water != WORKLOAD["n_water"]:  # smaller clusters for profiling captures
+        WORKLOAD.update(n_water=args.n_water, workload=f"(H2O){args.n_water} 6-31G** direct RHF", nbasis=25 * args.n_water)
     geom = water_cluster(WORKLOAD["n_water"], seed=WORKLOAD["seed"])
     fp32 = args.fp32_below
     # ---------------- warm-up SCF
@@ -356,6 +358,8 @@ def gpu_arm(args):
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches_per_build * builds, "wall_s": wall,
         "class_ms_per_build": {"%d%d%d%d" % c: float(x) / builds for c, x in zip(flop_model.CLASSES, class_ms)},
+        "class_counts_per_build": {"%d%d%d%d" % c: [float(v) / builds for v in row]
+                                   for c, row in zip(flop_model.CLASSES, counts)},
     }
     if rank == 0:
         print(json.dumps(line))
@@ -393,6 +397,7 @@ def main():
     ap.add_argument("--fp32-below", type=float, default=0.0, help="Schwarz bound below which quartets run in FP32")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge run")
+    ap.add_argument("--n-water", type=int, default=16, help="cluster size (16 = the benchmark workload)")
     ap.add_argument("--cpu-sample", metavar="SPEC")
     ap.add_argument("--cores", type=int, default=None)
     args = ap.parse_args()

@@ -190,6 +190,12 @@ struct mmdg_context {
   DevBuf<double> d_screen, d_sq;
   DevBuf<float> d_sqf, d_dPf, d_Dsh;
   DevBuf<unsigned long long> d_counters;
+  // quartet lists of the Fock build (allocated on first use): per class a region of
+  // capacity = number of candidate quartets, for FP64 and (on demand) FP32
+  std::vector<long long> q_off, q_cap;
+  long long q_total = 0;
+  DevBuf<int2> d_q64, d_q32;
+  DevBuf<unsigned> d_qn;  // [2*MMDG_NCLASS]: FP64 and FP32 list lengths
   Geometry geom() const {
     Geometry g;
     g.pP = d_pP.p;
@@ -639,22 +645,58 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   f.tolf_lo = float(tol * (1.0 - 1e-4));
   f.tolf_hi = float(tol * (1.0 + 1e-4));
   const float split = float(fp32_below);
+  // ---- quartet-list storage (first use)
+  if (h->q_off.empty()) {
+    h->q_off.assign(MMDG_NCLASS, 0);
+    h->q_cap.assign(MMDG_NCLASS, 0);
+    long long tot = 0;
+    int ci = 0;
+    for (const ClassEntry& e : kClasses) {
+      const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
+      const long long nb = h->cls_count[cb], nk = h->cls_count[ck];
+      const long long cap = cb == ck ? nb * (nb + 1) / 2 : nb * nk;
+      h->q_off[ci] = tot;
+      h->q_cap[ci] = cap;
+      tot += cap;
+      ++ci;
+    }
+    h->q_total = tot;
+    if (h->d_q64.alloc(tot > 0 ? tot : 1) != cudaSuccess || h->d_qn.alloc(2 * MMDG_NCLASS) != cudaSuccess) {
+      h->q_off.clear();
+      return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the quartet lists");
+    }
+  }
+  if (split > 0.f && !h->d_q32.p) {
+    if (h->d_q32.alloc(h->q_total > 0 ? h->q_total : 1) != cudaSuccess)
+      return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the FP32 quartet lists");
+  }
+  CUDA_TRY(cudaMemsetAsync(h->d_qn.p, 0, sizeof(unsigned) * 2 * MMDG_NCLASS, st));
   cudaEvent_t ev[2 * MMDG_NCLASS];
   if (class_ms)
     for (int k = 0; k < 2 * MMDG_NCLASS; ++k) CUDA_TRY(cudaEventCreate(&ev[k]));
+  // ---- screening passes (all classes), then evaluation
   int ci = 0;
+  for (const ClassEntry& e : kClasses) {
+    const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
+    if (h->cls_count[cb] && h->cls_count[ck]) {
+      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
+      QuartetLists ql{h->d_q64.p + h->q_off[ci], split > 0.f ? h->d_q32.p + h->q_off[ci] : nullptr,
+                      h->d_qn.p + ci, h->d_qn.p + MMDG_NCLASS + ci};
+      dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads);
+      k_screen<<<grid, kThreads, 0, st>>>(g, f, cl, ql);
+      CUDA_TRY(cudaGetLastError());
+    }
+    ++ci;
+  }
+  ci = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     f.counters = h->d_counters.p + 3 * ci;
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
     if (h->cls_count[cb] && h->cls_count[ck]) {
-      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, split, INFINITY};
-      CUDA_TRY(e.fock(0, g, f, cl, st));
-      if (split > 0.f) {
-        cl.qmin = 0.f;
-        cl.qmax = split;
-        CUDA_TRY(e.fock(1, g, f, cl, st));
-      }
+      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
+      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + ci, st));
+      if (split > 0.f) CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + MMDG_NCLASS + ci, st));
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;

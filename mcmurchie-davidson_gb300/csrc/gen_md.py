@@ -5,7 +5,8 @@ For every angular class (la lb|lc ld) with la>=lb, lc>=ld, (la,lb)>=(lc,ld)
 (lmax = 2: 21 classes) it emits one ``struct MD_<la><lb><lc><ld>`` whose
 ``run()`` evaluates one contracted shell quartet in straight-line code:
 
-    for each chunk of ket Cartesian function pairs (compile-time unrolled):
+    for each chunk of ket Cartesian function pairs (compile-time unrolled; a Fock
+    kernel thread evaluates one chunk of one quartet, ``c.chunk``; -1 = all):
       acc[ab][cd in chunk] = 0
       for each bra primitive pair i:
         W[cd in chunk][tuv] = 0                         (tuv: bra Hermite, t+u+v <= la+lb)
@@ -175,7 +176,8 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
     o.append(f"struct {name} {{")
     o.append(f"  static constexpr int LA = {la}, LB = {lb}, LC = {lc}, LD = {ld}, L = {L};")
     o.append(f"  static constexpr int NAB = {nab}, NCD = {ncd}, NNZ_AB = {nnz_ab}, NNZ_CD = {nnz_cd};")
-    o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = {chunk}, RSMEM = {smem};")
+    nchunk = -(-ncd // chunk)
+    o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = {chunk}, NCHUNK = {nchunk}, RSMEM = {smem};")
     o.append(f"  template <class Ctx, class Digest>")
     o.append(f"  static __device__ __forceinline__ void run(const Ctx& c, Digest& dg) {{")
     if smem:
@@ -186,8 +188,8 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
         o.append(f"    Real Rr[{H(L)}];")
         rvar = lambda k: f"Rr[{k}]"
     chunks = [list(range(s, min(s + chunk, ncd))) for s in range(0, ncd, chunk)]
-    for ch in chunks:
-        o.append(f"    {{ // ket function pairs {ch[0]}..{ch[-1]}")
+    for ci, ch in enumerate(chunks):
+        o.append(f"    if (c.chunk < 0 || c.chunk == {ci}) {{ // ket function pairs {ch[0]}..{ch[-1]}")
         for fab in range(nab):
             o.append("      Real " + ", ".join(f"a{fab}_{fcd} = 0" for fcd in ch) + ";")
         o.append(f"      for (int i = c.bra_begin; i < c.bra_end; ++i) {{")
@@ -262,14 +264,15 @@ def gen_class_compact(la, lb, lc, ld):
     o.append(f"struct {name} {{")
     o.append(f"  static constexpr int LA = {la}, LB = {lb}, LC = {lc}, LD = {ld}, L = {L};")
     o.append(f"  static constexpr int NAB = {nab}, NCD = {ncd}, NNZ_AB = {nnz_ab}, NNZ_CD = {nnz_cd};")
-    o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = 1, RSMEM = 1;")
+    o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = 1, NCHUNK = {ncd}, RSMEM = 1;")
     o.append(f"  template <class Ctx, class Digest>")
     o.append(f"  static __device__ __forceinline__ void run(const Ctx& c, Digest& dg) {{")
     o.append(f"    Real* __restrict__ Rs = c.template rsmem<Real>();")
     o.append(f"    const int RS = c.rstride();")
     rvar = lambda k: f"Rs[{k} * RS]"
+    o.append(f"    const int f0 = c.chunk < 0 ? 0 : c.chunk, f1 = c.chunk < 0 ? NCD : c.chunk + 1;")
     o.append(f"#pragma unroll 1")
-    o.append(f"    for (int fcd = 0; fcd < NCD; ++fcd) {{")
+    o.append(f"    for (int fcd = f0; fcd < f1; ++fcd) {{")
     o.append(f"      const int t0 = kTB_{s}[fcd], t1 = kTB_{s}[fcd + 1];")
     o.append("      Real " + ", ".join(f"a{fab} = 0" for fab in range(nab)) + ";")
     o.append(f"      for (int i = c.bra_begin; i < c.bra_end; ++i) {{")
@@ -346,7 +349,7 @@ def generate_instances(outdir, ngroups=6):
         load[k] += sz
     files = []
     decl = ["// Generated by gen_md.py -- do not edit.", "#pragma once", '#include "md_kernels.cuh"', "namespace mmdg {",
-            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, cudaStream_t);",
+            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
             "struct ClassEntry { int la, lb, lc, ld; fock_fn fock; tensor_fn tensor; schwarz_fn schwarz; };"]
@@ -354,7 +357,7 @@ def generate_instances(outdir, ngroups=6):
         decl.append(f"cudaError_t init_group{g}();")
     for c in cls:
         s = "".join(map(str, c))
-        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, cudaStream_t);")
+        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, cudaStream_t);")
         decl.append(f"cudaError_t launch_tensor_{s}(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);")
         if c[:2] == c[2:]:
             decl.append(f"cudaError_t launch_schwarz_{s}(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);")
@@ -374,10 +377,9 @@ def generate_instances(outdir, ngroups=6):
         for c in grp:
             s = "".join(map(str, c))
             md = f"MD_{s}"
-            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, cudaStream_t st) {{")
-            t.append(f"  dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads);")
-            t.append(f"  if (prec) k_fock<{md}<float>, float><<<grid, kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl);")
-            t.append(f"  else k_fock<{md}<double>, double><<<grid, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl);")
+            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, cudaStream_t st) {{")
+            t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>()), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count);")
+            t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>()), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_tensor_{s}(const Geometry& g, const TensorArgs& a, const ClassLaunch& cl, cudaStream_t st) {{")

@@ -149,6 +149,7 @@ struct Ctx;
 template <>
 struct Ctx<double> {
   const Geometry* g;
+  int chunk;  // ket chunk evaluated by this thread, -1 = all chunks
   int bra_begin, bra_end, ket_begin, ket_end;
   long long ebra, eket;
   int nnz_ab, nnz_cd;
@@ -189,6 +190,7 @@ struct Ctx<double> {
 template <>
 struct Ctx<float> {
   const Geometry* g;
+  int chunk;
   int bra_begin, bra_end, ket_begin, ket_end;
   long long ebra, eket;
   int nnz_ab, nnz_cd;

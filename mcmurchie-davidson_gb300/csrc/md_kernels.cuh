@@ -18,7 +18,7 @@ struct ClassLaunch {
   const int* ket;   // shell-pair indices of the ket class list
   int nbra, nket;
   int same;         // bra class == ket class: only ket slot <= bra slot
-  float qmin, qmax; // compute only quartets with qmin <= Q_bra*Q_ket < qmax (precision split)
+  float qmin, qmax; // screening pass: quartets with Q_bra*Q_ket < qmax go to the FP32 list
 };
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
@@ -27,6 +27,7 @@ template <class MD, typename Real>
 __device__ __forceinline__ Ctx<Real> make_ctx(const Geometry& g, int bp, int kp, Real* rs) {
   Ctx<Real> c;
   c.g = &g;
+  c.chunk = -1;
   c.bra_begin = __ldg(g.pr_begin + bp);
   c.bra_end = c.bra_begin + __ldg(g.pr_count + bp);
   c.ket_begin = __ldg(g.pr_begin + kp);
@@ -40,8 +41,31 @@ __device__ __forceinline__ Ctx<Real> make_ctx(const Geometry& g, int bp, int kp,
   return c;
 }
 
-template <class MD, typename Real>
-__global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl) {
+// Screening pass of one class pair: every candidate (bra slot, ket slot) is tested
+// against the shell-level bound Q_ab Q_cd max(4D_ab, 4D_cd, D_ac, D_ad, D_bc, D_bd)
+// (an upper bound of formPT's function-level test, fock.pyx:46-57) and appended to
+// the FP64 or the FP32 list of the class (warp-aggregated atomics), so that the
+// evaluation kernels run full warps.
+struct QuartetLists {
+  int2* q64;
+  int2* q32;
+  unsigned* n64;
+  unsigned* n32;
+};
+
+__device__ __forceinline__ void warp_append(bool keep, int2 v, int2* out, unsigned* n) {
+  const unsigned act = __activemask();
+  const unsigned b = __ballot_sync(act, keep);
+  if (!b) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(act) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(n, (unsigned)__popc(b));
+  base = __shfl_sync(act, base, leader);
+  if (keep) out[base + __popc(b & ((1u << lane) - 1u))] = v;
+}
+
+static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs f, ClassLaunch cl, QuartetLists ql) {
   const int ib = blockIdx.x;
   const int jk = blockIdx.y * kThreads + threadIdx.x;
   if (ib >= cl.nbra || jk >= cl.nket) return;
@@ -49,10 +73,9 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
   const int bp = __ldg(cl.bra + ib), kp = __ldg(cl.ket + jk);
   const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
   const int mol = __ldg(g.sh_mol + sa);
-  bool work = __ldg(g.sh_mol + sc) == mol;
+  bool keep = __ldg(g.sh_mol + sc) == mol;
   const float qq = __ldg(g.Q + bp) * __ldg(g.Q + kp);
-  work = work && qq >= cl.qmin && qq < cl.qmax;
-  if (work) {
+  if (keep) {
     const float* D = f.Dsh + g.mol_sbase[mol];
     const int S = g.mol_ns[mol];
     const int a = __ldg(g.sh_local + sa), b = __ldg(g.sh_local + sb);
@@ -60,25 +83,47 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
     const float dm = fmaxf(4.0f * fmaxf(__ldg(D + a * S + b), __ldg(D + c * S + d)),
                            fmaxf(fmaxf(__ldg(D + a * S + c), __ldg(D + a * S + d)),
                                  fmaxf(__ldg(D + b * S + c), __ldg(D + b * S + d))));
-    work = qq * dm >= f.tolf_lo;
+    keep = qq * dm >= f.tolf_lo;
   }
+  const bool lo = qq < cl.qmax;  // qmax carries the FP32 split (0: none)
+  const int2 v = make_int2(ib, jk);
+  warp_append(keep && !lo, v, ql.q64, ql.n64);
+  if (ql.q32) warp_append(keep && lo, v, ql.q32, ql.n32);
+}
+
+// Evaluation of a quartet list: persistent grid-stride loop over (chunk, quartet),
+// chunk-major so that a warp shares its chunk (and so its code path).
+template <class MD, typename Real>
+__global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
+                                                   const unsigned* count) {
+  const unsigned n = *count;
+  const long long total = (long long)n * MD::NCHUNK;
+  extern __shared__ double smem_d[];
+  Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
   unsigned nfq = 0, nsq = 0, npq = 0;
-  if (work) {
-    extern __shared__ double smem_d[];
-    Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
+  for (long long idx = blockIdx.x * (long long)kThreads + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * kThreads) {
+    const int chunk = (int)(idx / n);
+    const int qi = (int)(idx - (long long)chunk * n);
+    const int2 e = list[qi];
+    const int bp = __ldg(cl.bra + e.x), kp = __ldg(cl.ket + e.y);
+    const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
     Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, rs);
-    QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, mol};
+    c.chunk = MD::NCHUNK > 1 ? chunk : -1;
+    QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, __ldg(g.sh_mol + sa)};
     FockDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, f, q);
     MD::run(c, dg);
-    nfq = dg.nfq;
-    nsq = 1;
-    npq = unsigned((c.bra_end - c.bra_begin) * (c.ket_end - c.ket_begin));
+    nfq += dg.nfq;
+    if (chunk == 0) {
+      ++nsq;
+      npq += unsigned((c.bra_end - c.bra_begin) * (c.ket_end - c.ket_begin));
+    }
   }
   if (f.counters) {
     const unsigned mask = __activemask();
     const unsigned s0 = __reduce_add_sync(mask, nfq), s1 = __reduce_add_sync(mask, nsq),
                    s2 = __reduce_add_sync(mask, npq);
-    if ((threadIdx.x & 31) == __ffs(mask) - 1 && s1) {
+    if ((threadIdx.x & 31) == __ffs(mask) - 1 && (s0 | s1 | s2)) {
       atomicAdd(f.counters + 0, (unsigned long long)s0);
       atomicAdd(f.counters + 1, (unsigned long long)s1);
       atomicAdd(f.counters + 2, (unsigned long long)s2);
@@ -124,4 +169,16 @@ constexpr size_t smem_bytes() {
   return MD::RSMEM ? size_t(MD::HL) * kThreads * sizeof(Real) : 0;
 }
 
+}  // namespace mmdg
+
+namespace mmdg {
+// blocks of a persistent launch: every SM filled to the kernel's occupancy
+template <typename K>
+inline int persistent_blocks(K kernel, size_t smem) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, smem);
+  return sms * (per > 0 ? per : 1);
+}
 }  // namespace mmdg
