@@ -195,7 +195,14 @@ struct mmdg_context {
   std::vector<long long> q_off, q_cap;
   long long q_total = 0;
   DevBuf<int2> d_q64, d_q32;
-  DevBuf<unsigned> d_qn;  // [2*MMDG_NCLASS]: FP64 and FP32 list lengths
+  // buckets: per pair-class list, slots grouped by primitive count; per class
+  // (bra group, ket group) buckets with their offsets inside the class region
+  std::vector<int> ngroup;
+  DevBuf<int> d_gslot[kNumPairClasses];
+  std::vector<int> kbase, nkeys;
+  int total_keys = 0;
+  DevBuf<long long> d_keyoff;
+  DevBuf<unsigned> d_qn;  // [2*total_keys]: FP64 and FP32 bucket lengths
   Geometry geom() const {
     Geometry g;
     g.pP = d_pP.p;
@@ -534,6 +541,22 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
     h->cls_count[c] = (int)v.size();
     if (h->d_cls[c].upload(v) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
   }
+  // primitive-count groups of every class list (contiguous after the sort)
+  h->ngroup.assign(kNumPairClasses, 0);
+  for (int c = 0; c < kNumPairClasses; ++c) {
+    const std::vector<int>& v = lists[c];
+    std::vector<int> gs(v.size());
+    int gcount = 0;
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (i > 0 && h->pr_count[v[i]] != h->pr_count[v[i - 1]]) ++gcount;
+      gs[i] = gcount;
+    }
+    h->ngroup[c] = v.empty() ? 0 : gcount + 1;
+    if (h->d_gslot[c].upload(gs) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+  }
+  h->q_off.clear();
+  h->d_q64.release();
+  h->d_q32.release();
   CUDA_TRY(cudaDeviceSynchronize());
   h->have_basis = true;
   return MMDG_OK;
@@ -645,23 +668,52 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   f.tolf_lo = float(tol * (1.0 - 1e-4));
   f.tolf_hi = float(tol * (1.0 + 1e-4));
   const float split = float(fp32_below);
-  // ---- quartet-list storage (first use)
+  // ---- quartet-list storage (first use): per class, buckets (bra group, ket group)
   if (h->q_off.empty()) {
     h->q_off.assign(MMDG_NCLASS, 0);
     h->q_cap.assign(MMDG_NCLASS, 0);
+    h->kbase.assign(MMDG_NCLASS, 0);
+    h->nkeys.assign(MMDG_NCLASS, 0);
+    std::vector<long long> koff;
+    std::vector<std::vector<long long>> gsize(kNumPairClasses);
+    for (int c = 0; c < kNumPairClasses; ++c) {
+      gsize[c].assign(h->ngroup[c], 0);
+      std::vector<int> gs(h->cls_count[c]);
+      if (h->cls_count[c]) CUDA_TRY(cudaMemcpy(gs.data(), h->d_gslot[c].p, sizeof(int) * gs.size(), cudaMemcpyDeviceToHost));
+      for (int x : gs) gsize[c][x]++;
+    }
     long long tot = 0;
-    int ci = 0;
+    int ci = 0, nk = 0;
     for (const ClassEntry& e : kClasses) {
       const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
-      const long long nb = h->cls_count[cb], nk = h->cls_count[ck];
-      const long long cap = cb == ck ? nb * (nb + 1) / 2 : nb * nk;
+      const int Gb = h->ngroup[cb], Gk = h->ngroup[ck];
       h->q_off[ci] = tot;
-      h->q_cap[ci] = cap;
-      tot += cap;
+      h->kbase[ci] = nk;
+      h->nkeys[ci] = Gb * Gk;
+      if (Gb * Gk > kMaxKeys) {
+        h->q_off.clear();
+        return fail(MMDG_E_ARG, "mmdg_fock: too many primitive-count groups in one class");
+      }
+      long long rel = 0;
+      for (int gb = 0; gb < Gb; ++gb)
+        for (int gk = 0; gk < Gk; ++gk) {
+          long long cap;
+          if (cb != ck) cap = gsize[cb][gb] * gsize[ck][gk];
+          else if (gk < gb) cap = gsize[cb][gb] * gsize[ck][gk];
+          else if (gk == gb) cap = gsize[cb][gb] * (gsize[cb][gb] + 1) / 2;
+          else cap = 0;
+          koff.push_back(rel);
+          rel += cap;
+        }
+      h->q_cap[ci] = rel;
+      tot += rel;
+      nk += Gb * Gk;
       ++ci;
     }
     h->q_total = tot;
-    if (h->d_q64.alloc(tot > 0 ? tot : 1) != cudaSuccess || h->d_qn.alloc(2 * MMDG_NCLASS) != cudaSuccess) {
+    h->total_keys = nk;
+    if (h->d_q64.alloc(tot > 0 ? tot : 1) != cudaSuccess || h->d_qn.alloc(2 * (nk > 0 ? nk : 1)) != cudaSuccess ||
+        h->d_keyoff.upload(koff) != cudaSuccess) {
       h->q_off.clear();
       return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the quartet lists");
     }
@@ -670,7 +722,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     if (h->d_q32.alloc(h->q_total > 0 ? h->q_total : 1) != cudaSuccess)
       return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the FP32 quartet lists");
   }
-  CUDA_TRY(cudaMemsetAsync(h->d_qn.p, 0, sizeof(unsigned) * 2 * MMDG_NCLASS, st));
+  CUDA_TRY(cudaMemsetAsync(h->d_qn.p, 0, sizeof(unsigned) * 2 * (h->total_keys > 0 ? h->total_keys : 1), st));
   cudaEvent_t ev[2 * MMDG_NCLASS];
   if (class_ms)
     for (int k = 0; k < 2 * MMDG_NCLASS; ++k) CUDA_TRY(cudaEventCreate(&ev[k]));
@@ -680,8 +732,15 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     if (h->cls_count[cb] && h->cls_count[ck]) {
       ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
-      QuartetLists ql{h->d_q64.p + h->q_off[ci], split > 0.f ? h->d_q32.p + h->q_off[ci] : nullptr,
-                      h->d_qn.p + ci, h->d_qn.p + MMDG_NCLASS + ci};
+      QuartetLists ql{h->d_q64.p + h->q_off[ci],
+                      split > 0.f ? h->d_q32.p + h->q_off[ci] : nullptr,
+                      h->d_qn.p + h->kbase[ci],
+                      h->d_qn.p + h->total_keys + h->kbase[ci],
+                      h->d_keyoff.p + h->kbase[ci],
+                      h->d_gslot[cb].p,
+                      h->d_gslot[ck].p,
+                      h->ngroup[ck],
+                      h->nkeys[ci]};
       dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads);
       k_screen<<<grid, kThreads, 0, st>>>(g, f, cl, ql);
       CUDA_TRY(cudaGetLastError());
@@ -695,8 +754,11 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
     if (h->cls_count[cb] && h->cls_count[ck]) {
       ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
-      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + ci, st));
-      if (split > 0.f) CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + MMDG_NCLASS + ci, st));
+      const long long* ko = h->d_keyoff.p + h->kbase[ci];
+      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], st));
+      if (split > 0.f)
+        CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + h->total_keys + h->kbase[ci], ko,
+                        h->nkeys[ci], st));
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;

@@ -44,25 +44,32 @@ __device__ __forceinline__ Ctx<Real> make_ctx(const Geometry& g, int bp, int kp,
 // Screening pass of one class pair: every candidate (bra slot, ket slot) is tested
 // against the shell-level bound Q_ab Q_cd max(4D_ab, 4D_cd, D_ac, D_ad, D_bc, D_bd)
 // (an upper bound of formPT's function-level test, fock.pyx:46-57) and appended to
-// the FP64 or the FP32 list of the class (warp-aggregated atomics), so that the
-// evaluation kernels run full warps.
+// the FP64 or the FP32 list of the class.  Each list is split into buckets keyed by
+// (bra primitive-count group, ket primitive-count group), so that the 32 quartets a
+// warp evaluates together have the same primitive loop trip counts.
 struct QuartetLists {
-  int2* q64;
-  int2* q32;
-  unsigned* n64;
+  int2* q64;                  // class region (FP64)
+  int2* q32;                  // class region (FP32) or null
+  unsigned* n64;              // bucket lengths [nkeys]
   unsigned* n32;
+  const long long* key_off;   // bucket offsets within the class region [nkeys]
+  const int* gbra;            // slot -> primitive-count group, bra class list
+  const int* gket;            // same for the ket class list
+  int nkg;                    // groups of the ket class list
+  int nkeys;
 };
 
-__device__ __forceinline__ void warp_append(bool keep, int2 v, int2* out, unsigned* n) {
+__device__ __forceinline__ void bucket_append(bool keep, int key, int2 v, int2* out, unsigned* n,
+                                              const long long* key_off) {
   const unsigned act = __activemask();
-  const unsigned b = __ballot_sync(act, keep);
-  if (!b) return;
+  const unsigned peers = __match_any_sync(act, keep ? key : -1);
+  if (!keep) return;
   const int lane = threadIdx.x & 31;
-  const int leader = __ffs(act) - 1;
+  const int leader = __ffs(peers) - 1;
   unsigned base = 0;
-  if (lane == leader) base = atomicAdd(n, (unsigned)__popc(b));
-  base = __shfl_sync(act, base, leader);
-  if (keep) out[base + __popc(b & ((1u << lane) - 1u))] = v;
+  if (lane == leader) base = atomicAdd(n + key, (unsigned)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  out[key_off[key] + base + __popc(peers & ((1u << lane) - 1u))] = v;
 }
 
 static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs f, ClassLaunch cl, QuartetLists ql) {
@@ -86,26 +93,45 @@ static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs
     keep = qq * dm >= f.tolf_lo;
   }
   const bool lo = qq < cl.qmax;  // qmax carries the FP32 split (0: none)
+  const int key = __ldg(ql.gbra + ib) * ql.nkg + __ldg(ql.gket + jk);
   const int2 v = make_int2(ib, jk);
-  warp_append(keep && !lo, v, ql.q64, ql.n64);
-  if (ql.q32) warp_append(keep && lo, v, ql.q32, ql.n32);
+  bucket_append(keep && !lo, key, v, ql.q64, ql.n64, ql.key_off);
+  if (ql.q32) bucket_append(keep && lo, key, v, ql.q32, ql.n32, ql.key_off);
 }
 
-// Evaluation of a quartet list: persistent grid-stride loop over (chunk, quartet),
-// chunk-major so that a warp shares its chunk (and so its code path).
+constexpr int kMaxKeys = 256;
+
+// Evaluation of a bucketed quartet list: persistent grid-stride loop over
+// (chunk, bucket, quartet), chunk-major, so that a warp shares its chunk (code
+// path) and, inside a bucket, its primitive trip counts.
 template <class MD, typename Real>
 __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
-                                                   const unsigned* count) {
-  const unsigned n = *count;
+                                                   const unsigned* count, const long long* key_off, int nkeys) {
+  __shared__ unsigned s_pre[kMaxKeys + 1];
+  __shared__ long long s_off[kMaxKeys];
+  if (threadIdx.x == 0) {
+    unsigned acc = 0;
+    for (int k = 0; k < nkeys; ++k) {
+      s_pre[k] = acc;
+      s_off[k] = key_off[k];
+      acc += count[k];
+    }
+    s_pre[nkeys] = acc;
+  }
+  __syncthreads();
+  const unsigned n = s_pre[nkeys];
   const long long total = (long long)n * MD::NCHUNK;
   extern __shared__ double smem_d[];
   Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
   unsigned nfq = 0, nsq = 0, npq = 0;
+  int key = 0;
   for (long long idx = blockIdx.x * (long long)kThreads + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * kThreads) {
     const int chunk = (int)(idx / n);
-    const int qi = (int)(idx - (long long)chunk * n);
-    const int2 e = list[qi];
+    const unsigned r = (unsigned)(idx - (long long)chunk * n);
+    if (r < s_pre[key]) key = 0;
+    while (r >= s_pre[key + 1]) ++key;
+    const int2 e = list[s_off[key] + (r - s_pre[key])];
     const int bp = __ldg(cl.bra + e.x), kp = __ldg(cl.ket + e.y);
     const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
     Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, rs);
