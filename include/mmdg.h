@@ -115,6 +115,12 @@ int mmdg_fock_timed(mmdg_context* ctx, const double* dP, double* G, double tol, 
  * Measurement support; no counterpart in the reference. */
 int mmdg_measure_peaks(mmdg_context* ctx, double* fp64_tflops, double* fp32_tflops);
 
+/* Host copy of the Boys interpolation table (no GPU needed): rows (k, L) of
+ * F_{L+n}(k/16)/n! (n = 0..6, 8 doubles per row, L = 0..8, k = 0..767) followed by
+ * rows k of exp(-k/16)/n! (n = 0..7).  With out = NULL returns the length; else
+ * fills out[0..n) and returns the length, or a negative error code.  Test support. */
+long long mmdg_boys_table(double* out, long long n);
+
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
 

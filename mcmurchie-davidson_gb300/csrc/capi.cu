@@ -115,27 +115,35 @@ dd dd_exp_m16() {
 }  // namespace
 
 static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) {
-  t64.assign(kBoysNGrid * kBoysNCol, 0.0);
-  t32.assign(kBoysNGrid * kBoysNCol, 0.0f);
+  t64.assign(kBoysTabSize, 0.0);
+  t32.assign(kBoysTabSize, 0.0f);
   const dd e16 = dd_exp_m16();
   dd eT{1.0, 0.0};
-  const int mtop = kBoysNCol - 2;  // 14
+  const int mtop = kBoysLMax + 6;  // F_0 .. F_14
+  double fact[8] = {1, 1, 2, 6, 24, 120, 720, 5040};
   for (int k = 0; k < kBoysNGrid; ++k) {
     if (k > 0) eT = dd_mul(eT, e16);
     const double T = k / 16.0;
     // series at m = mtop
     dd term{1.0, 0.0}, sum{1.0, 0.0};
     const double b = mtop + 1.5;
-    for (int i = 0; i < 2000; ++i) {
+    for (int i = 0; i < 4000; ++i) {
       term = dd_div_d(dd_mul_d(term, T), b + i);
       sum = dd_add(sum, term);
       if (term.hi < sum.hi * 1e-34) break;
     }
-    dd F[kBoysNCol];
+    dd F[mtop + 1];
     F[mtop] = dd_div_d(dd_mul(eT, sum), 2.0 * mtop + 1.0);
     for (int m = mtop; m > 0; --m) F[m - 1] = dd_div_d(dd_add(dd_mul_d(F[m], 2.0 * T), eT), 2.0 * m - 1.0);
-    for (int m = 0; m <= mtop; ++m) t64[k * kBoysNCol + m] = F[m].hi + F[m].lo;
-    t64[k * kBoysNCol + kBoysNCol - 1] = eT.hi + eT.lo;
+    for (int L = 0; L <= kBoysLMax; ++L)
+      for (int n = 0; n < 7; ++n) {
+        const dd v = dd_div_d(F[L + n], fact[n]);
+        t64[(k * (kBoysLMax + 1) + L) * kBoysRow + n] = v.hi + v.lo;
+      }
+    for (int n = 0; n < 8; ++n) {
+      const dd v = dd_div_d(eT, fact[n]);
+      t64[kBoysExpOff + k * kBoysRow + n] = v.hi + v.lo;
+    }
   }
   for (size_t i = 0; i < t64.size(); ++i) t32[i] = float(t64[i]);
 }
@@ -1214,4 +1222,15 @@ extern "C" int mmdg_measure_peaks(mmdg_context* h, double* fp64_tflops, double* 
   cudaEventDestroy(e1);
   CUDA_TRY(cudaGetLastError());
   return MMDG_OK;
+}
+
+// host copy of the Boys interpolation table (no GPU needed): for tests
+extern "C" long long mmdg_boys_table(double* out, long long n) {
+  if (!out) return kBoysTabSize;
+  if (n < kBoysTabSize) return fail(MMDG_E_ARG, "mmdg_boys_table: buffer too small");
+  std::vector<double> t64;
+  std::vector<float> t32;
+  build_boys_table(t64, t32);
+  std::memcpy(out, t64.data(), sizeof(double) * kBoysTabSize);
+  return kBoysTabSize;
 }

@@ -2,7 +2,7 @@
 //
 // Numerics restate the reference (jjgoings/McMurchie-Davidson):
 //   * Boys function F_m(T) (cython/util.pxi:54-55) by tabulated Taylor interpolation
-//     plus downward recursion F_{m-1} = (2T F_m + e^{-T})/(2m-1); for T >= 36 the
+//     plus downward recursion F_{m-1} = (2T F_m + e^{-T})/(2m-1); for T >= 48 the
 //     asymptotic F_0 = sqrt(pi/T)/2 and upward recursion F_{m+1} = ((2m+1)F_m - e^{-T})/(2T).
 //   * R^(n)_000 = (-2 alpha)^n F_n(alpha |PQ|^2) (cython/util.pxi:37-38) with the
 //     prefactor 2 pi^{5/2} / (p q sqrt(p+q)) (cython/twoe.pyx:93) folded in.
@@ -21,9 +21,12 @@
 namespace mmdg {
 
 constexpr int kMaxComp = 6;         // Cartesian components of a d shell
-constexpr int kBoysNGrid = 576;     // T_k = k/16, k = 0..575
-constexpr int kBoysNCol = 16;       // F_0..F_14(T_k), exp(-T_k)
-constexpr double kBoysTaylorMax = 36.0 - 1.0 / 32.0;
+constexpr int kBoysNGrid = 768;     // T_k = k/16, k = 0..767 (T < 48)
+constexpr int kBoysLMax = 8;        // highest order the ERI classes need ((dd|dd))
+constexpr int kBoysRow = 8;         // doubles per (k, L) Taylor row (7 used)
+constexpr int kBoysExpOff = kBoysNGrid * (kBoysLMax + 1) * kBoysRow;  // exp rows after the F rows
+constexpr int kBoysTabSize = kBoysExpOff + kBoysNGrid * kBoysRow;
+constexpr double kBoysTaylorMax = 48.0 - 1.0 / 32.0;
 constexpr double kTwoPi52 = 34.986836655249725;  // 2 pi^{5/2}
 constexpr double kHalfSqrtPi = 0.88622692545275801;
 
@@ -53,52 +56,57 @@ struct Geometry {
   const int* __restrict__ mol_ns;            // S_m
   const long long* __restrict__ mol_tbase;   // offset of the molecule's N(N+1)/2 pair table
   // Boys tables
-  const double* __restrict__ boys64;  // [kBoysNGrid*kBoysNCol]
+  const double* __restrict__ boys64;  // [kBoysTabSize]
   const float* __restrict__ boys32;
 };
 
 // ---------------------------------------------------------------------------------
 // Boys function: Fn[0..L] at T
+// Table layout: row (k, L) holds c_n = F_{L+n}(T_k) / n!, n = 0..6, so that
+//   F_L(T) = sum_n c_n y^n,  y = T_k - T,  |y| <= 1/32,
+// and row (k, exp) holds e_n = exp(-T_k) / n!, n = 0..7, for exp(-T) = sum_n e_n y^n.
+// Truncation: F_{L+7} |y|^7 / 7! < 6e-15 F_L and |y|^8/8! < 3e-17 relative.
 template <int L>
 __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double T, double* Fn) {
   if (T < kBoysTaylorMax) {
     int k = __double2int_rn(T * 16.0);
     k = min(max(k, 0), kBoysNGrid - 1);
-    const double* __restrict__ row = tab + k * kBoysNCol;
-    const double y = fma(double(k), 0.0625, -T);  // -(T - T_k), |y| <= 1/32
-    const double y2 = y * 0.5, y3 = y * (1.0 / 3.0), y4 = y * 0.25, y5 = y * 0.2, y6 = y * (1.0 / 6.0);
-    // F_L(T) = sum_{n=0}^{6} F_{L+n}(T_k) y^n / n!  (Horner in y/n)
-    double f = row[L + 6];
-    f = fma(f, y6, row[L + 5]);
-    f = fma(f, y5, row[L + 4]);
-    f = fma(f, y4, row[L + 3]);
-    f = fma(f, y3, row[L + 2]);
-    f = fma(f, y2, row[L + 1]);
-    f = fma(f, y, row[L]);
-    Fn[L] = f;
+    const double y = fma(double(k), 0.0625, -T);  // T_k - T
+    const double* __restrict__ c = tab + (k * (kBoysLMax + 1) + L) * kBoysRow;
+    double f = fma(c[6], y, c[5]);
+    f = fma(f, y, c[4]);
+    f = fma(f, y, c[3]);
+    f = fma(f, y, c[2]);
+    f = fma(f, y, c[1]);
+    Fn[L] = fma(f, y, c[0]);
     if (L > 0) {
-      // exp(-T) = exp(-T_k) * exp(y), Taylor to y^7 / 7!
-      const double y7 = y * (1.0 / 7.0);
-      double e = fma(y7, 1.0, 1.0);
-      e = fma(e, y6, 1.0);
-      e = fma(e, y5, 1.0);
-      e = fma(e, y4, 1.0);
-      e = fma(e, y3, 1.0);
-      e = fma(e, y2, 1.0);
-      e = fma(e, y, 1.0);
-      const double eT = e * row[kBoysNCol - 1];
+      const double* __restrict__ e = tab + kBoysExpOff + k * kBoysRow;
+      double x = fma(e[7], y, e[6]);
+      x = fma(x, y, e[5]);
+      x = fma(x, y, e[4]);
+      x = fma(x, y, e[3]);
+      x = fma(x, y, e[2]);
+      x = fma(x, y, e[1]);
+      const double eT = fma(x, y, e[0]);
       const double T2 = T + T;
 #pragma unroll
       for (int m = L; m > 0; --m) Fn[m - 1] = fma(T2, Fn[m], eT) * (1.0 / double(2 * m - 1));
     }
   } else {
+    // F_0 = sqrt(pi/T)/2 and F_{m+1} = ((2m+1) F_m - exp(-T)) / (2T); for T >= 48 and
+    // m <= 4 the exp(-T) terms change F_m by less than 5e-15 relative and are dropped
     const double rs = rsqrt(T);
     Fn[0] = kHalfSqrtPi * rs;
     if (L > 0) {
-      const double eTh = 0.5 * exp(-T);
       const double iT = rs * rs;
+      if (L > 4) {
+        const double eTh = 0.5 * exp(-T);
 #pragma unroll
-      for (int m = 0; m < L; ++m) Fn[m + 1] = fma(double(m) + 0.5, Fn[m], -eTh) * iT;
+        for (int m = 0; m < L; ++m) Fn[m + 1] = fma(double(m) + 0.5, Fn[m], -eTh) * iT;
+      } else {
+#pragma unroll
+        for (int m = 0; m < L; ++m) Fn[m + 1] = (double(m) + 0.5) * iT * Fn[m];
+      }
     }
   }
 }
@@ -108,23 +116,18 @@ __device__ __forceinline__ void boys_eval(const float* __restrict__ tab, float T
   if (T < float(kBoysTaylorMax)) {
     int k = __float2int_rn(T * 16.0f);
     k = min(max(k, 0), kBoysNGrid - 1);
-    const float* __restrict__ row = tab + k * kBoysNCol;
     const float y = fmaf(float(k), 0.0625f, -T);
-    const float y2 = y * 0.5f, y3 = y * (1.0f / 3.0f), y4 = y * 0.25f;
-    float f = row[L + 4];
-    f = fmaf(f, y4, row[L + 3]);
-    f = fmaf(f, y3, row[L + 2]);
-    f = fmaf(f, y2, row[L + 1]);
-    f = fmaf(f, y, row[L]);
-    Fn[L] = f;
+    const float* __restrict__ c = tab + (k * (kBoysLMax + 1) + L) * kBoysRow;
+    float f = fmaf(c[4], y, c[3]);
+    f = fmaf(f, y, c[2]);
+    f = fmaf(f, y, c[1]);
+    Fn[L] = fmaf(f, y, c[0]);
     if (L > 0) {
-      const float y5 = y * 0.2f;
-      float e = fmaf(y5, 1.0f, 1.0f);
-      e = fmaf(e, y4, 1.0f);
-      e = fmaf(e, y3, 1.0f);
-      e = fmaf(e, y2, 1.0f);
-      e = fmaf(e, y, 1.0f);
-      const float eT = e * row[kBoysNCol - 1];
+      const float* __restrict__ e = tab + kBoysExpOff + k * kBoysRow;
+      float x = fmaf(e[4], y, e[3]);
+      x = fmaf(x, y, e[2]);
+      x = fmaf(x, y, e[1]);
+      const float eT = fmaf(x, y, e[0]);
       const float T2 = T + T;
 #pragma unroll
       for (int m = L; m > 0; --m) Fn[m - 1] = fmaf(T2, Fn[m], eT) * (1.0f / float(2 * m - 1));
@@ -133,10 +136,9 @@ __device__ __forceinline__ void boys_eval(const float* __restrict__ tab, float T
     const float rs = rsqrtf(T);
     Fn[0] = float(kHalfSqrtPi) * rs;
     if (L > 0) {
-      const float eTh = 0.5f * expf(-T);
       const float iT = rs * rs;
 #pragma unroll
-      for (int m = 0; m < L; ++m) Fn[m + 1] = fmaf(float(m) + 0.5f, Fn[m], -eTh) * iT;
+      for (int m = 0; m < L; ++m) Fn[m + 1] = (float(m) + 0.5f) * iT * Fn[m];
     }
   }
 }
@@ -305,22 +307,23 @@ struct FockDigest {
         if (f.sq[tbase + ij] * f.sq[tbase + kl] * d < f.tol) return;
       }
     }
-    double v = double(vr);
-    // degeneracy s12 * s34 * s12_34 (fock.pyx:60-70); powers of two
-    if (i != j) v += v;
-    if (k != l) v += v;
-    if (!(i == k && j == l)) v += v;
+    // degeneracy s12 * s34 * s12_34 in {1,2,4,8} (fock.pyx:60-70) and the exchange
+    // weight -1/4 are powers of two: applied exactly on the exponent field (integer
+    // pipe) instead of FP64 multiplies.  Values whose exponent field is below 64
+    // (|v| < 1e-289, zeros included) contribute nothing at double precision.
+    const long long bits = __double_as_longlong(double(vr));
+    if (((bits >> 52) & 0x7ff) < 64) { ++nfq; return; }
+    const long long deg = (long long)((i != j) + (k != l) + !(i == k && j == l));
+    const double v = __longlong_as_double(bits + (deg << 52));
+    const double vq = __longlong_as_double((bits + ((deg - 2) << 52)) ^ (long long)0x8000000000000000ULL);
     const double* dP = f.dP;
     double* G = f.G;
-    const long long rL = base + (long long)l * N;
     atomicAdd(G + rI + j, dP[rK + l] * v);
     atomicAdd(G + rK + l, dP[rI + j] * v);
-    const double vq = -0.25 * v;
     atomicAdd(G + rI + k, dP[rJ + l] * vq);
     atomicAdd(G + rJ + l, dP[rI + k] * vq);
     atomicAdd(G + rI + l, dP[rJ + k] * vq);
     atomicAdd(G + rK + j, dP[rI + l] * vq);
-    (void)rL;
     ++nfq;
   }
 };

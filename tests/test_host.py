@@ -83,7 +83,7 @@ def test_flop_model():
 
 def _header_symbols():
     txt = open(os.path.join(REPO, "include", "mmdg.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(mmdg_\w+)\s*\(", txt, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char\*)\s+(mmdg_\w+)\s*\(", txt, flags=re.M)))
 
 
 def test_capi_exports_every_declared_symbol(built_lib):
@@ -93,3 +93,29 @@ def test_capi_exports_every_declared_symbol(built_lib):
     assert "mmdg_fock" in syms and "mmdg_eri_tensor" in syms and len(syms) >= 10
     for s in syms:
         assert hasattr(lib, s), s
+
+
+def test_boys_table_vs_mpmath(built_lib):
+    """The GPU Boys table (built on the host in double-double arithmetic) is
+    correctly rounded: F_{L+n}(T_k)/n! and exp(-T_k)/n! against mpmath."""
+    import ctypes
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    lib = ctypes.CDLL(built_lib)
+    lib.mmdg_boys_table.restype = ctypes.c_longlong
+    lib.mmdg_boys_table.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
+    n = lib.mmdg_boys_table(None, 0)
+    tab = np.zeros(n)
+    assert lib.mmdg_boys_table(tab.ctypes.data, n) == n
+    ngrid, lmax, row = 768, 8, 8
+    fact = [1, 1, 2, 6, 24, 120, 720, 5040]
+    for k in (0, 1, 17, 100, 333, 500, 767):
+        T = mp.mpf(k) / 16
+        for L in (0, 1, 4, 8):
+            for nn in range(7):
+                m = L + nn
+                ex = mp.hyp1f1(m + mp.mpf(1) / 2, m + mp.mpf(3) / 2, -T) / (2 * m + 1) / fact[nn]
+                got = tab[(k * (lmax + 1) + L) * row + nn]
+                assert abs(got - float(ex)) <= 1.2e-16 * abs(float(ex)), (k, L, nn)
+        e = tab[ngrid * (lmax + 1) * row + k * row]
+        assert abs(e - float(mp.exp(-T))) <= 1.2e-16 * float(mp.exp(-T))
