@@ -300,6 +300,7 @@ def gpu_arm(args):
     dom_cls = flop_model.CLASSES[dom]
     achieved = cls_flops[dom] / (class_ms[dom] / 1e3) / 1e12
     build_ms = float(class_ms.sum()) / builds
+    step_other_ms = 1e3 * t_dev / builds - build_ms
     all_achieved = float(cls_flops.sum()) / (float(class_ms.sum()) / 1e3) / 1e12
     roofline = {"bound": "fp64", "kernel": "k_fock<MD_%d%d%d%d,double>" % dom_cls, "achieved": achieved,
                 "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
@@ -357,6 +358,7 @@ def gpu_arm(args):
         "e2e": e2e, "time_to_converge_s": ttc, "scf_iterations": iters, "energy": E,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches_per_build * builds, "wall_s": wall,
+        "step_breakdown_ms": {"fock_build_kernels": build_ms, "rest_of_step": step_other_ms},
         "class_ms_per_build": {"%d%d%d%d" % c: float(x) / builds for c, x in zip(flop_model.CLASSES, class_ms)},
         "class_counts_per_build": {"%d%d%d%d" % c: [float(v) / builds for v in row]
                                    for c, row in zip(flop_model.CLASSES, counts)},

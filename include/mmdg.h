@@ -115,7 +115,7 @@ int mmdg_fock_timed(mmdg_context* ctx, const double* dP, double* G, double tol, 
  * Measurement support; no counterpart in the reference. */
 int mmdg_measure_peaks(mmdg_context* ctx, double* fp64_tflops, double* fp32_tflops);
 
-/* Host copy of the Boys interpolation table (no GPU needed): rows (k, L) of
+/* Host copy of the Boys interpolation table (no GPU needed): rows (L, k) of
  * F_{L+n}(k/16)/n! (n = 0..6, 8 doubles per row, L = 0..8, k = 0..767) followed by
  * rows k of exp(-k/16)/n! (n = 0..7).  With out = NULL returns the length; else
  * fills out[0..n) and returns the length, or a negative error code.  Test support. */

@@ -138,7 +138,7 @@ static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) 
     for (int L = 0; L <= kBoysLMax; ++L)
       for (int n = 0; n < 7; ++n) {
         const dd v = dd_div_d(F[L + n], fact[n]);
-        t64[(k * (kBoysLMax + 1) + L) * kBoysRow + n] = v.hi + v.lo;
+        t64[(L * kBoysNGrid + k) * kBoysRow + n] = v.hi + v.lo;
       }
     for (int n = 0; n < 8; ++n) {
       const dd v = dd_div_d(eT, fact[n]);

@@ -195,6 +195,9 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
         o.append(f"      for (int i = c.bra_begin; i < c.bra_end; ++i) {{")
         for fcd in ch:
             o.append("        Real " + ", ".join(f"w{fcd}_{k} = 0" for k in range(len(hp))) + ";")
+        if not smem and L <= UNROLL_KET_MAX_L:
+            # two independent primitive quartets in flight: hides the Boys/rsqrt chains
+            o.append(f"#pragma unroll 2")
         o.append(f"        for (int j = c.ket_begin; j < c.ket_end; ++j) {{")
         o.append(f"          Real Rn[{L + 1}], X, Y, Z;")
         o.append(f"          c.template hermite_r0<{L}>(i, j, Rn, X, Y, Z);")
@@ -311,6 +314,8 @@ def gen_class_compact(la, lb, lc, ld):
 
 # classes with la+lb+lc+ld above this use the compact form
 COMPACT_ABOVE_L = 4
+# register-resident classes up to this total L unroll the ket primitive loop by two
+UNROLL_KET_MAX_L = 2
 
 
 def generate(path, overrides=None):

@@ -62,7 +62,8 @@ struct Geometry {
 
 // ---------------------------------------------------------------------------------
 // Boys function: Fn[0..L] at T
-// Table layout: row (k, L) holds c_n = F_{L+n}(T_k) / n!, n = 0..6, so that
+// Table layout (L-major, so one class touches a contiguous 48 KB): row (L, k)
+// holds c_n = F_{L+n}(T_k) / n!, n = 0..6, so that
 //   F_L(T) = sum_n c_n y^n,  y = T_k - T,  |y| <= 1/32,
 // and row (k, exp) holds e_n = exp(-T_k) / n!, n = 0..7, for exp(-T) = sum_n e_n y^n.
 // Truncation: F_{L+7} |y|^7 / 7! < 6e-15 F_L and |y|^8/8! < 3e-17 relative.
@@ -72,7 +73,7 @@ __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double
     int k = __double2int_rn(T * 16.0);
     k = min(max(k, 0), kBoysNGrid - 1);
     const double y = fma(double(k), 0.0625, -T);  // T_k - T
-    const double* __restrict__ c = tab + (k * (kBoysLMax + 1) + L) * kBoysRow;
+    const double* __restrict__ c = tab + (L * kBoysNGrid + k) * kBoysRow;
     double f = fma(c[6], y, c[5]);
     f = fma(f, y, c[4]);
     f = fma(f, y, c[3]);
@@ -117,7 +118,7 @@ __device__ __forceinline__ void boys_eval(const float* __restrict__ tab, float T
     int k = __float2int_rn(T * 16.0f);
     k = min(max(k, 0), kBoysNGrid - 1);
     const float y = fmaf(float(k), 0.0625f, -T);
-    const float* __restrict__ c = tab + (k * (kBoysLMax + 1) + L) * kBoysRow;
+    const float* __restrict__ c = tab + (L * kBoysNGrid + k) * kBoysRow;
     float f = fmaf(c[4], y, c[3]);
     f = fmaf(f, y, c[2]);
     f = fmaf(f, y, c[1]);

@@ -115,7 +115,7 @@ def test_boys_table_vs_mpmath(built_lib):
             for nn in range(7):
                 m = L + nn
                 ex = mp.hyp1f1(m + mp.mpf(1) / 2, m + mp.mpf(3) / 2, -T) / (2 * m + 1) / fact[nn]
-                got = tab[(k * (lmax + 1) + L) * row + nn]
+                got = tab[(L * ngrid + k) * row + nn]
                 assert abs(got - float(ex)) <= 1.2e-16 * abs(float(ex)), (k, L, nn)
         e = tab[ngrid * (lmax + 1) * row + k * row]
         assert abs(e - float(mp.exp(-T))) <= 1.2e-16 * float(mp.exp(-T))
