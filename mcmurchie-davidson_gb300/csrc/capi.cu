@@ -20,19 +20,24 @@
 using namespace mmdg;
 
 // ------------------------------------------------------------------ errors
-static thread_local std::string g_last_error;
+// fixed-size, so that recording an error never allocates
+static thread_local char g_last_error[512];
 
-static int fail(int code, const std::string& msg) {
-  g_last_error = msg;
+static int fail_c(int code, const char* msg) {
+  std::strncpy(g_last_error, msg, sizeof(g_last_error) - 1);
+  g_last_error[sizeof(g_last_error) - 1] = 0;
   return code;
 }
+static int fail(int code, const std::string& msg) { return fail_c(code, msg.c_str()); }
 #define CUDA_TRY(x)                                                                                  \
   do {                                                                                               \
     cudaError_t e_ = (x);                                                                            \
     if (e_ != cudaSuccess) return fail(MMDG_E_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
   } while (0)
 
-extern "C" const char* mmdg_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* mmdg_last_error(void) { return g_last_error; }
+
+int mmdg_internal_fail(int code, const char* msg) { return fail_c(code, msg); }
 
 // ------------------------------------------------------------------ device buffers
 template <typename T>
@@ -114,9 +119,9 @@ dd dd_exp_m16() {
 }
 }  // namespace
 
-static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) {
-  t64.assign(kBoysTabSize, 0.0);
-  t32.assign(kBoysTabSize, 0.0f);
+// Fills t64 (kBoysTabSize doubles) and, if non-null, t32; no heap allocation.
+static void build_boys_table_raw(double* t64, float* t32) {
+  for (int i = 0; i < kBoysTabSize; ++i) t64[i] = 0.0;
   const dd e16 = dd_exp_m16();
   dd eT{1.0, 0.0};
   const int mtop = kBoysLMax + 6;  // F_0 .. F_14
@@ -145,7 +150,14 @@ static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) 
       t64[kBoysExpOff + k * kBoysRow + n] = v.hi + v.lo;
     }
   }
-  for (size_t i = 0; i < t64.size(); ++i) t32[i] = float(t64[i]);
+  if (t32)
+    for (int i = 0; i < kBoysTabSize; ++i) t32[i] = float(t64[i]);
+}
+
+static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) {
+  t64.assign(kBoysTabSize, 0.0);
+  t32.assign(kBoysTabSize, 0.0f);
+  build_boys_table_raw(t64.data(), t32.data());
 }
 
 // ------------------------------------------------------------------ context
@@ -292,17 +304,7 @@ extern "C" int mmdg_destroy(mmdg_context* h) {
 // primitive normalisation of cython/basis.pxi:101-105.
 __device__ __forceinline__ double comp_norm(int l) { return l >= 2 ? 0.57735026918962576 : 1.0; }
 
-struct PairBuildArgs {
-  int npair;
-  const int *pa, *pb, *prb;
-  const long long* eoff;
-  const int *L, *nprim, *poff;
-  const double *center, *exps, *coefs;
-  double4_32a* pP;
-  float4* pPf;
-  double* E64;
-  float* E32;
-};
+#include "pairs.cuh"
 
 __global__ void k_build_pairs(PairBuildArgs a) {
   const int pr = blockIdx.x * blockDim.x + threadIdx.x;
@@ -330,7 +332,7 @@ __global__ void k_build_pairs(PairBuildArgs a) {
       const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * ip;
       const long long pp = a.prb[pr] + k;
       a.pP[pp] = make_double4_32a(p, Px, Py, Pz);
-      a.pPf[pp] = make_float4(float(p), float(Px), float(Py), float(Pz));
+      if (a.pPf) a.pPf[pp] = make_float4(float(p), float(Px), float(Py), float(Pz));
       // 1D tables E[d][i][j][t], i<=2, j<=2, t<=4
       double E[3][3][3][5];
       const double i2p = 0.5 * ip;
@@ -370,7 +372,7 @@ __global__ void k_build_pairs(PairBuildArgs a) {
                   for (int v = 0; v <= za + zb; ++v) {
                     const double e = c * E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][v];
                     a.E64[o] = e;
-                    a.E32[o] = float(e);
+                    if (a.E32) a.E32[o] = float(e);
                     ++o;
                   }
             }
@@ -1223,6 +1225,8 @@ extern "C" int mmdg_measure_peaks(mmdg_context* h, double* fp64_tflops, double* 
   CUDA_TRY(cudaGetLastError());
   return MMDG_OK;
 }
+
+void mmdg_fill_boys_table(double* t64) { build_boys_table_raw(t64, nullptr); }
 
 // host copy of the Boys interpolation table (no GPU needed): for tests
 extern "C" long long mmdg_boys_table(double* out, long long n) {
