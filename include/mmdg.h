@@ -144,6 +144,31 @@ int mmdg_one_electron(mmdg_context* ctx, int natom, const int* atom_mol, const d
                       const double* atom_Z, const double* origin, double* S, double* T, double* V, double* M,
                       void* stream);
 
+/*
+ * ERI tensor of one small molecule that allocates nothing -- no cudaMalloc, no
+ * cudaFree, no host heap.  No counterpart in the reference (it has no device
+ * memory to manage); this is mmdg_eri_tensor for callers that cannot allocate:
+ * host frameworks that own the whole GPU memory pool and forbid outside
+ * allocations, code that must not synchronise the device (cudaMalloc/cudaFree can),
+ * and services that cannot recover from an allocation failure mid-request.
+ *
+ * Same basis arguments as mmdg_set_basis for one molecule (nfunc functions; no
+ * context needed) and a caller-owned device output `out` of nfunc^4 doubles.
+ * All scratch (Boys table, primitive pairs, E' tables, bookkeeping) lives in one
+ * static device array of 1,738,240 bytes that every GPU loading the library holds
+ * until the process exits.  Limits: 64 shells, 64 functions, 256 primitives, 4096
+ * primitive pairs, 131072 E' coefficients, l <= 2; larger inputs fail with
+ * MMDG_E_ARG and a message naming the limit.  The first call on a device (the
+ * device current) looks up the array's device address and uploads the Boys table;
+ * make that first call before any stream capture.  Every call shares the array:
+ * calls that overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  The call synchronises `stream` once while staging
+ * its inputs.
+ */
+int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int* shell_nprim, const double* shell_center,
+                            const double* prim_exp, const double* prim_coef, const int* shell_func, int nfunc,
+                            double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
