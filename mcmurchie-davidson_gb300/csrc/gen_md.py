@@ -198,9 +198,13 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
         if not smem and L <= UNROLL_KET_MAX_L:
             # two independent primitive quartets in flight: hides the Boys/rsqrt chains
             o.append(f"#pragma unroll 2")
+        o.append(f"        const auto ap = c.pp(i);")
+        o.append(f"        auto bq = c.pp(c.ket_begin);")
         o.append(f"        for (int j = c.ket_begin; j < c.ket_end; ++j) {{")
+        o.append(f"          const auto bp = bq;")
+        o.append(f"          if (j + 1 < c.ket_end) bq = c.pp(j + 1);  // next ket primitive pair, one iteration ahead")
         o.append(f"          Real Rn[{L + 1}], X, Y, Z;")
-        o.append(f"          c.template hermite_r0<{L}>(i, j, Rn, X, Y, Z);")
+        o.append(f"          c.template hermite_r0_pp<{L}>(ap, bp, Rn, X, Y, Z);")
         if L == 0:
             o.append(f"          {rvar(0)} = Rn[0];")
         else:
@@ -280,9 +284,13 @@ def gen_class_compact(la, lb, lc, ld):
     o.append("      Real " + ", ".join(f"a{fab} = 0" for fab in range(nab)) + ";")
     o.append(f"      for (int i = c.bra_begin; i < c.bra_end; ++i) {{")
     o.append("        Real " + ", ".join(f"w{k} = 0" for k in range(len(hp))) + ";")
+    o.append(f"        const auto ap = c.pp(i);")
+    o.append(f"        auto bq = c.pp(c.ket_begin);")
     o.append(f"        for (int j = c.ket_begin; j < c.ket_end; ++j) {{")
+    o.append(f"          const auto bp = bq;")
+    o.append(f"          if (j + 1 < c.ket_end) bq = c.pp(j + 1);")
     o.append(f"          Real Rn[{L + 1}], X, Y, Z;")
-    o.append(f"          c.template hermite_r0<{L}>(i, j, Rn, X, Y, Z);")
+    o.append(f"          c.template hermite_r0_pp<{L}>(ap, bp, Rn, X, Y, Z);")
     o.append(f"          {rvar(0)} = Rn[{L}];")
     emit_r_recursion(L, rvar, o, "          ")
     o.append(f"          const Real* __restrict__ ek = c.ket_E(j);")

@@ -168,10 +168,15 @@ struct Ctx<double> {
   __device__ __forceinline__ const double* bra_E(int i) const {
     return g->E64 + ebra + (long long)(i - bra_begin) * nnz_ab;
   }
+  typedef double4_32a PP;
+  __device__ __forceinline__ PP pp(int k) const { return g->pP[k]; }
   template <int L>
   __device__ __forceinline__ void hermite_r0(int i, int j, double* Rn, double& X, double& Y, double& Z) const {
-    const double4_32a a = g->pP[i];
-    const double4_32a b = g->pP[j];
+    hermite_r0_pp<L>(g->pP[i], g->pP[j], Rn, X, Y, Z);
+  }
+  template <int L>
+  __device__ __forceinline__ void hermite_r0_pp(const PP& a, const PP& b, double* Rn, double& X, double& Y,
+                                                double& Z) const {
     X = a.y - b.y;
     Y = a.z - b.z;
     Z = a.w - b.w;
@@ -209,19 +214,26 @@ struct Ctx<float> {
   __device__ __forceinline__ const float* bra_E(int i) const {
     return g->E32 + ebra + (long long)(i - bra_begin) * nnz_ab;
   }
+  struct PP {
+    double4_32a d;  // P in FP64: P - Q needs the precision
+    float p;        // exponent sum in FP32
+  };
+  __device__ __forceinline__ PP pp(int k) const { return PP{g->pP[k], g->pPf[k].x}; }
   template <int L>
   __device__ __forceinline__ void hermite_r0(int i, int j, float* Rn, float& X, float& Y, float& Z) const {
+    hermite_r0_pp<L>(pp(i), pp(j), Rn, X, Y, Z);
+  }
+  template <int L>
+  __device__ __forceinline__ void hermite_r0_pp(const PP& a, const PP& b, float* Rn, float& X, float& Y,
+                                                float& Z) const {
     // P - Q in FP64 (coordinates of ~10 bohr would lose the difference in FP32)
-    const double4_32a a = g->pP[i];
-    const double4_32a b = g->pP[j];
-    X = float(a.y - b.y);
-    Y = float(a.z - b.z);
-    Z = float(a.w - b.w);
-    const float4 af = g->pPf[i];
-    const float4 bf = g->pPf[j];
+    X = float(a.d.y - b.d.y);
+    Y = float(a.d.z - b.d.z);
+    Z = float(a.d.w - b.d.w);
     const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
-    const float rsum = rsqrtf(af.x + bf.x);
-    const float alpha = af.x * bf.x * (rsum * rsum);
+    const float pa = a.p, pb = b.p;
+    const float rsum = rsqrtf(pa + pb);
+    const float alpha = pa * pb * (rsum * rsum);
     float F[L + 1];
     boys_eval<L>(g->boys32, alpha * r2, F);
     float c = float(kTwoPi52) * rsum;
