@@ -332,7 +332,11 @@ __global__ void k_build_pairs(PairBuildArgs a) {
       const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * ip;
       const long long pp = a.prb[pr] + k;
       a.pP[pp] = make_double4_32a(p, Px, Py, Pz);
-      if (a.pPf) a.pPf[pp] = make_float4(float(p), float(Px), float(Py), float(Pz));
+      if (a.pPf) {
+        const float hx = float(Px), hy = float(Py), hz = float(Pz);
+        a.pPf[2 * pp] = make_float4(float(p), hx, hy, hz);
+        a.pPf[2 * pp + 1] = make_float4(0.f, float(Px - hx), float(Py - hy), float(Pz - hz));
+      }
       // 1D tables E[d][i][j][t], i<=2, j<=2, t<=4
       double E[3][3][3][5];
       const double i2p = 0.5 * ip;
@@ -487,7 +491,7 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
             h->d_pa.upload(h->pa) == cudaSuccess && h->d_pb.upload(h->pb) == cudaSuccess &&
             h->d_prb.upload(h->pr_begin) == cudaSuccess && h->d_prc.upload(h->pr_count) == cudaSuccess &&
             h->d_eoff.upload(h->e_off) == cudaSuccess && h->d_pP.alloc(npp) == cudaSuccess &&
-            h->d_pPf.alloc(npp) == cudaSuccess && h->d_E64.alloc(ne) == cudaSuccess &&
+            h->d_pPf.alloc(2 * npp) == cudaSuccess && h->d_E64.alloc(ne) == cudaSuccess &&
             h->d_E32.alloc(ne) == cudaSuccess && h->d_Q.alloc(h->npair) == cudaSuccess &&
             h->d_screen.alloc(tt) == cudaSuccess && h->d_sq.alloc(tt) == cudaSuccess &&
             h->d_sqf.alloc(tt) == cudaSuccess && h->d_dPf.alloc(nn) == cudaSuccess &&

@@ -35,7 +35,7 @@ constexpr double kHalfSqrtPi = 0.88622692545275801;
 struct Geometry {
   // primitive pairs
   const double4_32a* __restrict__ pP;   // (p, Px, Py, Pz) per primitive pair
-  const float4* __restrict__ pPf;   // same in FP32
+  const float4* __restrict__ pPf;   // FP32: (p, Px, Py, Pz) rounded, then (0, Px, Py, Pz) remainders: 2 per pair
   const double* __restrict__ E64;   // E' tables, FP64
   const float* __restrict__ E32;    // E' tables, FP32
   // shell pairs
@@ -215,10 +215,10 @@ struct Ctx<float> {
     return g->E32 + ebra + (long long)(i - bra_begin) * nnz_ab;
   }
   struct PP {
-    double4_32a d;  // P in FP64: P - Q needs the precision
-    float p;        // exponent sum in FP32
+    float4 hi;  // (p, P) rounded to FP32
+    float4 lo;  // (0, P - hi): P as an unevaluated float pair
   };
-  __device__ __forceinline__ PP pp(int k) const { return PP{g->pP[k], g->pPf[k].x}; }
+  __device__ __forceinline__ PP pp(int k) const { return PP{g->pPf[2 * k], g->pPf[2 * k + 1]}; }
   template <int L>
   __device__ __forceinline__ void hermite_r0(int i, int j, float* Rn, float& X, float& Y, float& Z) const {
     hermite_r0_pp<L>(pp(i), pp(j), Rn, X, Y, Z);
@@ -226,12 +226,13 @@ struct Ctx<float> {
   template <int L>
   __device__ __forceinline__ void hermite_r0_pp(const PP& a, const PP& b, float* Rn, float& X, float& Y,
                                                 float& Z) const {
-    // P - Q in FP64 (coordinates of ~10 bohr would lose the difference in FP32)
-    X = float(a.d.y - b.d.y);
-    Y = float(a.d.z - b.d.z);
-    Z = float(a.d.w - b.d.w);
+    // P - Q from float pairs (hi + lo): the difference keeps FP32 relative precision
+    // even for nearby centres ~10 bohr from the origin, without any FP64 instruction
+    X = (a.hi.y - b.hi.y) + (a.lo.y - b.lo.y);
+    Y = (a.hi.z - b.hi.z) + (a.lo.z - b.lo.z);
+    Z = (a.hi.w - b.hi.w) + (a.lo.w - b.lo.w);
     const float r2 = fmaf(X, X, fmaf(Y, Y, Z * Z));
-    const float pa = a.p, pb = b.p;
+    const float pa = a.hi.x, pb = b.hi.x;
     const float rsum = rsqrtf(pa + pb);
     const float alpha = pa * pb * (rsum * rsum);
     float F[L + 1];

@@ -234,3 +234,25 @@ def test_fock_counts_and_linearity():
     # with tol = 0 every unique function quartet is digested: N(N+1)/2 pairs, triangle
     npair = N * (N + 1) // 2
     assert int(c1[:, 0].sum()) == npair * (npair + 1) // 2
+
+
+def test_mixed_precision_fock_and_energy():
+    """FP32 for shell quartets with Schwarz bound below 1e-5 (FP64 for the rest, for
+    the Boys branches' inputs of large-bound quartets, Fock accumulation, DIIS,
+    eigensolve and energy): per-build max |dF| and the final energy against the
+    all-FP64 path on a seeded (H2O)4 / 6-31G** cluster."""
+    import torch
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    geom = water_cluster(4, seed=3)
+    m64 = Molecule(geom, "6-31gss")
+    E64 = m64.RHF(doPrint=False, direct=True)
+    m32 = Molecule(geom, "6-31gss")
+    E32 = m32.RHF(doPrint=False, direct=True, fp32_below=1e-5)
+    assert abs(E32 - E64) < 1e-8, (E32, E64)
+    # one full build on the converged density: max element error of G
+    ctx = m64.context
+    P = torch.tensor(m64.P, device="cuda").reshape(-1).contiguous()
+    G64 = ctx.fock(P, tol=1e-12).clone()
+    G32 = ctx.fock(P, tol=1e-12, fp32_below=1e-5)
+    assert torch.max(torch.abs(G64 - G32)).item() < 1e-9
