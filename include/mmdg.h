@@ -121,6 +121,21 @@ int mmdg_measure_peaks(mmdg_context* ctx, double* fp64_tflops, double* fp32_tflo
  * fills out[0..n) and returns the length, or a negative error code.  Test support. */
 long long mmdg_boys_table(double* out, long long n);
 
+/* Autotuner hooks (no counterpart in the reference).  mmdg_set_tuning sets the
+ * persistent grid of angular class `cls` (0..MMDG_NCLASS-1, the order of the class
+ * table: (ss|ss), (ps|ss), (ps|ps), (pp|ss), ...; 0 = one full wave at the kernel's
+ * occupancy); mmdg_set_streams spreads the class kernels over 1..4 concurrent
+ * streams (fork/join on events). */
+int mmdg_set_tuning(mmdg_context* ctx, int cls, int grid_blocks);
+int mmdg_set_streams(mmdg_context* ctx, int nstreams);
+
+/* mmdg_fock replayed as one CUDA graph: the first call with a given (dP, G, tol,
+ * fp32_below) runs the build eagerly and captures its launches (screening, class
+ * kernels over all molecules, memsets) into a graph; later calls with the same
+ * arguments launch that graph on `stream`.  Used by the batched SCF, where one
+ * launch serves every molecule of the batch. */
+int mmdg_fock_graph(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below, void* stream);
+
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
 

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -154,10 +155,19 @@ static void build_boys_table_raw(double* t64, float* t32) {
     for (int i = 0; i < kBoysTabSize; ++i) t32[i] = float(t64[i]);
 }
 
+// computed once per process (every context uploads the same table)
 static void build_boys_table(std::vector<double>& t64, std::vector<float>& t32) {
-  t64.assign(kBoysTabSize, 0.0);
-  t32.assign(kBoysTabSize, 0.0f);
-  build_boys_table_raw(t64.data(), t32.data());
+  static std::mutex mu;
+  static std::vector<double> c64;
+  static std::vector<float> c32;
+  std::lock_guard<std::mutex> lock(mu);
+  if (c64.empty()) {
+    c64.assign(kBoysTabSize, 0.0);
+    c32.assign(kBoysTabSize, 0.0f);
+    build_boys_table_raw(c64.data(), c32.data());
+  }
+  t64 = c64;
+  t32 = c32;
 }
 
 // ------------------------------------------------------------------ context
@@ -206,6 +216,21 @@ struct mmdg_context {
   // class lists (sorted by primitive count, then Q descending)
   std::vector<int> cls_count;
   DevBuf<int> d_cls[kNumPairClasses];
+  DevBuf<int> d_cls_moff[kNumPairClasses];  // per class list: slot offset of every molecule [nmol+1]
+  std::vector<std::vector<long long>> bucket_cap;  // per angular class: capacity of every bucket
+  std::vector<long long> mol_shell0;        // first global shell of every molecule
+  DevBuf<long long> d_mol_shell0;
+  // tuning (autotuner): persistent grid per class (0 = occupancy), concurrent class streams
+  int class_grid[MMDG_NCLASS] = {0};
+  int nstreams = 1;
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // CUDA graph of one Fock build (mmdg_fock_graph)
+  cudaGraphExec_t graph = nullptr;
+  const double* g_dP = nullptr;
+  double* g_G = nullptr;
+  double g_tol = -1.0, g_split = -1.0;
+  cudaStream_t g_stream = nullptr;
   // screening / Fock scratch
   DevBuf<double> d_screen, d_sq;
   DevBuf<float> d_sqf, d_dPf, d_Dsh;
@@ -289,6 +314,13 @@ extern "C" int mmdg_create(mmdg_context** out, int device) {
 extern "C" int mmdg_destroy(mmdg_context* h) {
   if (!h) return MMDG_OK;
   DeviceGuard dg(h->device);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (int k = 0; k < 4; ++k) {
+    if (h->side[k]) cudaStreamDestroy(h->side[k]);
+    if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
+  }
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
+  if (h->g_stream) cudaStreamDestroy(h->g_stream);
   delete h;
   return MMDG_OK;
 }
@@ -542,31 +574,74 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
     k_sqrt_screen<<<(unsigned)((n + 255) / 256), 256>>>(h->d_screen.p, h->d_sq.p, h->d_sqf.p, n);
     CUDA_TRY(cudaGetLastError());
   }
-  // ---- sorted class lists: primitive count ascending, Q descending
+  // ---- sorted class lists: molecule, primitive count ascending, Q descending
   std::vector<float> Q(h->npair);
   CUDA_TRY(cudaMemcpy(Q.data(), h->d_Q.p, sizeof(float) * h->npair, cudaMemcpyDeviceToHost));
   h->cls_count.assign(kNumPairClasses, 0);
+  h->ngroup.assign(kNumPairClasses, 0);
+  std::vector<std::vector<int>> slot_group(kNumPairClasses), slot_mol(kNumPairClasses);
   for (int c = 0; c < kNumPairClasses; ++c) {
     std::vector<int>& v = lists[c];
     std::stable_sort(v.begin(), v.end(), [&](int x, int y) {
+      const int mx = shell_mol[h->pa[x]], my = shell_mol[h->pa[y]];
+      if (mx != my) return mx < my;
       if (h->pr_count[x] != h->pr_count[y]) return h->pr_count[x] < h->pr_count[y];
       return Q[x] > Q[y];
     });
     h->cls_count[c] = (int)v.size();
     if (h->d_cls[c].upload(v) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
-  }
-  // primitive-count groups of every class list (contiguous after the sort)
-  h->ngroup.assign(kNumPairClasses, 0);
-  for (int c = 0; c < kNumPairClasses; ++c) {
-    const std::vector<int>& v = lists[c];
-    std::vector<int> gs(v.size());
-    int gcount = 0;
+    // molecule offsets within the list
+    std::vector<int> moff(nmol + 1, 0);
+    for (int x : v) moff[shell_mol[h->pa[x]] + 1]++;
+    for (int m = 0; m < nmol; ++m) moff[m + 1] += moff[m];
+    if (h->d_cls_moff[c].upload(moff) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+    // primitive-count groups: rank of the pair's primitive count among the class's values
+    std::vector<int> vals;
+    for (int x : v) vals.push_back(h->pr_count[x]);
+    std::sort(vals.begin(), vals.end());
+    vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
+    std::vector<int> gs(v.size()), ms(v.size());
     for (size_t i = 0; i < v.size(); ++i) {
-      if (i > 0 && h->pr_count[v[i]] != h->pr_count[v[i - 1]]) ++gcount;
-      gs[i] = gcount;
+      gs[i] = int(std::lower_bound(vals.begin(), vals.end(), h->pr_count[v[i]]) - vals.begin());
+      ms[i] = shell_mol[h->pa[v[i]]];
     }
-    h->ngroup[c] = v.empty() ? 0 : gcount + 1;
+    h->ngroup[c] = (int)vals.size();
     if (h->d_gslot[c].upload(gs) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+    slot_group[c] = gs;
+    slot_mol[c] = ms;
+  }
+  // bucket capacities per angular class: sum over molecules of the candidate counts
+  {
+    h->bucket_cap.assign(MMDG_NCLASS, {});
+    int ci = 0;
+    for (const ClassEntry& e : kClasses) {
+      const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
+      const int Gb = h->ngroup[cb], Gk = h->ngroup[ck];
+      std::vector<long long> cap((size_t)Gb * Gk, 0);
+      // per molecule group sizes
+      std::vector<long long> nb((size_t)nmol * (Gb ? Gb : 1), 0), nk((size_t)nmol * (Gk ? Gk : 1), 0);
+      for (size_t i = 0; i < slot_group[cb].size(); ++i) nb[(size_t)slot_mol[cb][i] * Gb + slot_group[cb][i]]++;
+      for (size_t i = 0; i < slot_group[ck].size(); ++i) nk[(size_t)slot_mol[ck][i] * Gk + slot_group[ck][i]]++;
+      for (int m = 0; m < nmol; ++m)
+        for (int gb = 0; gb < Gb; ++gb)
+          for (int gk = 0; gk < Gk; ++gk) {
+            const long long a = nb[(size_t)m * Gb + gb], b = nk[(size_t)m * Gk + gk];
+            long long c2;
+            if (cb != ck || gk < gb) c2 = a * b;
+            else if (gk == gb) c2 = a * (a + 1) / 2;
+            else c2 = 0;
+            cap[(size_t)gb * Gk + gk] += c2;
+          }
+      h->bucket_cap[ci] = cap;
+      ++ci;
+    }
+  }
+  h->mol_shell0.assign(nmol, 0);
+  for (int s = nshell - 1; s >= 0; --s) h->mol_shell0[shell_mol[s]] = s;
+  if (h->d_mol_shell0.upload(h->mol_shell0) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
   }
   h->q_off.clear();
   h->d_q64.release();
@@ -612,29 +687,36 @@ __global__ void k_prep_density(const double* dP, float* dPf, long long n) {
   dPf[i] = float(fabs(dP[i]));
 }
 
-// per-molecule S x S block maxima of |dP| (one thread per shell pair block)
-__global__ void k_shell_dmax(const float* dPf, float* Dsh, const int* func, const int* L, const int* sh_mol,
-                             const int* sh_local, const long long* mol_base, const int* mol_n,
-                             const long long* mol_sbase, const int* mol_ns, int nshell) {
+// per-molecule S x S block maxima of |dP|: one thread per (molecule, shell, shell)
+__global__ void k_shell_dmax(const float* dPf, float* Dsh, const int* func, const int* L,
+                             const long long* mol_base, const int* mol_n, const long long* mol_sbase,
+                             const int* mol_ns, const long long* mol_shell0, int nmol, long long total) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const int s1 = (int)(idx / nshell), s2 = (int)(idx % nshell);
-  if (s1 >= nshell) return;
-  const int m = sh_mol[s1];
-  if (sh_mol[s2] != m) return;
-  const int N = mol_n[m], S = mol_ns[m];
+  if (idx >= total) return;
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (mol_sbase[mid] <= idx) lo = mid;
+    else hi = mid - 1;
+  }
+  const int m = lo;
+  const int S = mol_ns[m], N = mol_n[m];
+  const long long loc = idx - mol_sbase[m];
+  const int a = (int)(loc / S), b = (int)(loc % S);
+  const int s1 = (int)(mol_shell0[m] + a), s2 = (int)(mol_shell0[m] + b);
   const float* D = dPf + mol_base[m];
   const int n1 = (L[s1] + 1) * (L[s1] + 2) / 2, n2 = (L[s2] + 1) * (L[s2] + 2) / 2;
   float mx = 0.f;
-  for (int a = 0; a < n1; ++a) {
-    const int i = func[s1 * kMaxComp + a];
+  for (int x = 0; x < n1; ++x) {
+    const int i = func[s1 * kMaxComp + x];
     if (i < 0) continue;
-    for (int b = 0; b < n2; ++b) {
-      const int j = func[s2 * kMaxComp + b];
+    for (int y = 0; y < n2; ++y) {
+      const int j = func[s2 * kMaxComp + y];
       if (j < 0) continue;
       mx = fmaxf(mx, D[(long long)i * N + j]);
     }
   }
-  Dsh[mol_sbase[m] + (long long)sh_local[s1] * S + sh_local[s2]] = mx;
+  Dsh[idx] = mx;
 }
 
 static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
@@ -664,10 +746,10 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   k_prep_density<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(dP, h->d_dPf.p, nn);
   CUDA_TRY(cudaGetLastError());
   {
-    const long long n = (long long)h->nshell * h->nshell;
+    const long long n = h->ntot_ss;
     k_shell_dmax<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->d_dPf.p, h->d_Dsh.p, h->d_func.p, h->d_L.p,
-                                                              h->d_shmol.p, h->d_shlocal.p, h->d_mol_base.p,
-                                                              h->d_mol_n.p, h->d_mol_sbase.p, h->d_mol_ns.p, h->nshell);
+                                                              h->d_mol_base.p, h->d_mol_n.p, h->d_mol_sbase.p,
+                                                              h->d_mol_ns.p, h->d_mol_shell0.p, h->nmol, n);
     CUDA_TRY(cudaGetLastError());
   }
   Geometry g = h->geom();
@@ -689,45 +771,27 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     h->kbase.assign(MMDG_NCLASS, 0);
     h->nkeys.assign(MMDG_NCLASS, 0);
     std::vector<long long> koff;
-    std::vector<std::vector<long long>> gsize(kNumPairClasses);
-    for (int c = 0; c < kNumPairClasses; ++c) {
-      gsize[c].assign(h->ngroup[c], 0);
-      std::vector<int> gs(h->cls_count[c]);
-      if (h->cls_count[c]) CUDA_TRY(cudaMemcpy(gs.data(), h->d_gslot[c].p, sizeof(int) * gs.size(), cudaMemcpyDeviceToHost));
-      for (int x : gs) gsize[c][x]++;
-    }
     long long tot = 0;
-    int ci = 0, nk = 0;
-    for (const ClassEntry& e : kClasses) {
-      const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
-      const int Gb = h->ngroup[cb], Gk = h->ngroup[ck];
+    int nk = 0;
+    for (int ci = 0; ci < MMDG_NCLASS; ++ci) {
+      const std::vector<long long>& cap = h->bucket_cap[ci];
+      if ((int)cap.size() > kMaxKeys) return fail(MMDG_E_ARG, "mmdg_fock: too many primitive-count groups in one class");
       h->q_off[ci] = tot;
       h->kbase[ci] = nk;
-      h->nkeys[ci] = Gb * Gk;
-      if (Gb * Gk > kMaxKeys) {
-        h->q_off.clear();
-        return fail(MMDG_E_ARG, "mmdg_fock: too many primitive-count groups in one class");
-      }
+      h->nkeys[ci] = (int)cap.size();
       long long rel = 0;
-      for (int gb = 0; gb < Gb; ++gb)
-        for (int gk = 0; gk < Gk; ++gk) {
-          long long cap;
-          if (cb != ck) cap = gsize[cb][gb] * gsize[ck][gk];
-          else if (gk < gb) cap = gsize[cb][gb] * gsize[ck][gk];
-          else if (gk == gb) cap = gsize[cb][gb] * (gsize[cb][gb] + 1) / 2;
-          else cap = 0;
-          koff.push_back(rel);
-          rel += cap;
-        }
+      for (long long c2 : cap) {
+        koff.push_back(rel);
+        rel += c2;
+      }
       h->q_cap[ci] = rel;
       tot += rel;
-      nk += Gb * Gk;
-      ++ci;
+      nk += (int)cap.size();
     }
     h->q_total = tot;
     h->total_keys = nk;
     if (h->d_q64.alloc(tot > 0 ? tot : 1) != cudaSuccess || h->d_qn.alloc(2 * (nk > 0 ? nk : 1)) != cudaSuccess ||
-        h->d_keyoff.upload(koff) != cudaSuccess) {
+        h->d_keyoff.upload(koff.empty() ? std::vector<long long>{0} : koff) != cudaSuccess) {
       h->q_off.clear();
       return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the quartet lists");
     }
@@ -745,7 +809,8 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     if (h->cls_count[cb] && h->cls_count[ck]) {
-      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
+      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split,
+                     h->d_cls_moff[ck].p};
       QuartetLists ql{h->d_q64.p + h->q_off[ci],
                       split > 0.f ? h->d_q32.p + h->q_off[ci] : nullptr,
                       h->d_qn.p + h->kbase[ci],
@@ -755,28 +820,43 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
                       h->d_gslot[ck].p,
                       h->ngroup[ck],
                       h->nkeys[ci]};
-      dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads);
-      k_screen<<<grid, kThreads, 0, st>>>(g, f, cl, ql);
+      k_screen<<<cl.nbra, kThreads, 0, st>>>(g, f, cl, ql);
       CUDA_TRY(cudaGetLastError());
     }
     ++ci;
   }
+  // class kernels, optionally spread over concurrent streams (fork / join on events)
+  const int ns = class_ms ? 1 : h->nstreams;
+  if (ns > 1) {
+    CUDA_TRY(cudaEventRecord(h->fork_ev, st));
+    for (int k = 0; k < ns; ++k) CUDA_TRY(cudaStreamWaitEvent(h->side[k], h->fork_ev, 0));
+  }
   ci = 0;
+  int launched = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     f.counters = h->d_counters.p + 3 * ci;
+    cudaStream_t cs = ns > 1 ? h->side[launched % ns] : st;
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
     if (h->cls_count[cb] && h->cls_count[ck]) {
-      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split};
+      ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split,
+                     h->d_cls_moff[ck].p};
       const long long* ko = h->d_keyoff.p + h->kbase[ci];
-      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], st));
+      const int grid = h->class_grid[ci];
+      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], grid, cs));
       if (split > 0.f)
         CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + h->total_keys + h->kbase[ci], ko,
-                        h->nkeys[ci], st));
+                        h->nkeys[ci], grid, cs));
+      ++launched;
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;
   }
+  if (ns > 1)
+    for (int k = 0; k < ns; ++k) {
+      CUDA_TRY(cudaEventRecord(h->join_ev[k], h->side[k]));
+      CUDA_TRY(cudaStreamWaitEvent(st, h->join_ev[k], 0));
+    }
   if (class_ms) {
     CUDA_TRY(cudaEventSynchronize(ev[2 * MMDG_NCLASS - 1]));
     for (int k = 0; k < MMDG_NCLASS; ++k) CUDA_TRY(cudaEventElapsedTime(&class_ms[k], ev[2 * k], ev[2 * k + 1]));
@@ -1241,4 +1321,72 @@ extern "C" long long mmdg_boys_table(double* out, long long n) {
   build_boys_table(t64, t32);
   std::memcpy(out, t64.data(), sizeof(double) * kBoysTabSize);
   return kBoysTabSize;
+}
+
+// ------------------------------------------------------------------ tuning, CUDA graph
+extern "C" int mmdg_set_tuning(mmdg_context* h, int cls, int grid_blocks) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_tuning: null context");
+  if (cls < 0 || cls >= MMDG_NCLASS || grid_blocks < 0) return fail(MMDG_E_ARG, "mmdg_set_tuning: bad class or grid");
+  h->class_grid[cls] = grid_blocks;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return MMDG_OK;
+}
+
+extern "C" int mmdg_set_streams(mmdg_context* h, int nstreams) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_streams: null context");
+  if (nstreams < 1 || nstreams > 4) return fail(MMDG_E_ARG, "mmdg_set_streams: 1 to 4 streams");
+  DeviceGuard dg(h->device);
+  if (!h->fork_ev) CUDA_TRY(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
+  for (int k = 0; k < nstreams; ++k) {
+    if (!h->side[k]) CUDA_TRY(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking));
+    if (!h->join_ev[k]) CUDA_TRY(cudaEventCreateWithFlags(&h->join_ev[k], cudaEventDisableTiming));
+  }
+  h->nstreams = nstreams;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return MMDG_OK;
+}
+
+extern "C" int mmdg_fock_graph(mmdg_context* h, const double* dP, double* G, double tol, double fp32_below,
+                               void* stream) {
+  if (!h || !dP || !G) return fail(MMDG_E_ARG, "mmdg_fock_graph: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_fock_graph: no basis set");
+  DeviceGuard dgd(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool same = h->graph && h->g_dP == dP && h->g_G == G && h->g_tol == tol && h->g_split == fp32_below;
+  if (!same) {
+    if (h->graph) {
+      cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+    }
+    // first build eagerly: allocates the quartet lists outside any capture
+    int rc = fock_impl(h, dP, G, tol, fp32_below, nullptr, nullptr, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (!h->g_stream) CUDA_TRY(cudaStreamCreateWithFlags(&h->g_stream, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(h->g_stream, cudaStreamCaptureModeThreadLocal));
+    rc = fock_impl(h, dP, G, tol, fp32_below, nullptr, nullptr, h->g_stream);
+    cudaError_t e = cudaStreamEndCapture(h->g_stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(MMDG_E_CUDA, std::string("mmdg_fock_graph: capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(MMDG_E_CUDA, std::string("mmdg_fock_graph: instantiate: ") + cudaGetErrorString(e));
+    h->g_dP = dP;
+    h->g_G = G;
+    h->g_tol = tol;
+    h->g_split = fp32_below;
+    return MMDG_OK;  // this call's build ran eagerly above
+  }
+  CUDA_TRY(cudaGraphLaunch(h->graph, st));
+  return MMDG_OK;
 }

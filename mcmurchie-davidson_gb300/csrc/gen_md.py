@@ -362,7 +362,7 @@ def generate_instances(outdir, ngroups=6):
         load[k] += sz
     files = []
     decl = ["// Generated by gen_md.py -- do not edit.", "#pragma once", '#include "md_kernels.cuh"', "namespace mmdg {",
-            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, cudaStream_t);",
+            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
             "struct ClassEntry { int la, lb, lc, ld; fock_fn fock; tensor_fn tensor; schwarz_fn schwarz; };"]
@@ -370,7 +370,7 @@ def generate_instances(outdir, ngroups=6):
         decl.append(f"cudaError_t init_group{g}();")
     for c in cls:
         s = "".join(map(str, c))
-        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, cudaStream_t);")
+        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);")
         decl.append(f"cudaError_t launch_tensor_{s}(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);")
         if c[:2] == c[2:]:
             decl.append(f"cudaError_t launch_schwarz_{s}(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);")
@@ -390,9 +390,9 @@ def generate_instances(outdir, ngroups=6):
         for c in grp:
             s = "".join(map(str, c))
             md = f"MD_{s}"
-            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, const long long* koff, int nkeys, cudaStream_t st) {{")
-            t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>()), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count, koff, nkeys);")
-            t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>()), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count, koff, nkeys);")
+            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, const long long* koff, int nkeys, int grid, cudaStream_t st) {{")
+            t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>(), grid), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count, koff, nkeys);")
+            t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>(), grid), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count, koff, nkeys);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_tensor_{s}(const Geometry& g, const TensorArgs& a, const ClassLaunch& cl, cudaStream_t st) {{")

@@ -19,6 +19,7 @@ struct ClassLaunch {
   int nbra, nket;
   int same;         // bra class == ket class: only ket slot <= bra slot
   float qmin, qmax; // screening pass: quartets with Q_bra*Q_ket < qmax go to the FP32 list
+  const int* kmoff; // ket list: slot offset of every molecule (lists are molecule-major)
 };
 
 __host__ __device__ constexpr int ncart(int l) { return (l + 1) * (l + 2) / 2; }
@@ -72,31 +73,45 @@ __device__ __forceinline__ void bucket_append(bool keep, int key, int2 v, int2* 
   out[key_off[key] + base + __popc(peers & ((1u << lane) - 1u))] = v;
 }
 
+// One block per bra slot; its threads walk the ket slots of the same molecule (the
+// lists are molecule-major), so a batch of molecules never forms cross-molecule
+// candidates.
 static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs f, ClassLaunch cl, QuartetLists ql) {
   const int ib = blockIdx.x;
-  const int jk = blockIdx.y * kThreads + threadIdx.x;
-  if (ib >= cl.nbra || jk >= cl.nket) return;
-  if (cl.same && jk > ib) return;
-  const int bp = __ldg(cl.bra + ib), kp = __ldg(cl.ket + jk);
-  const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
+  if (ib >= cl.nbra) return;
+  const int bp = __ldg(cl.bra + ib);
+  const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp);
   const int mol = __ldg(g.sh_mol + sa);
-  bool keep = __ldg(g.sh_mol + sc) == mol;
-  const float qq = __ldg(g.Q + bp) * __ldg(g.Q + kp);
-  if (keep) {
-    const float* D = f.Dsh + g.mol_sbase[mol];
-    const int S = g.mol_ns[mol];
-    const int a = __ldg(g.sh_local + sa), b = __ldg(g.sh_local + sb);
-    const int c = __ldg(g.sh_local + sc), d = __ldg(g.sh_local + sd);
-    const float dm = fmaxf(4.0f * fmaxf(__ldg(D + a * S + b), __ldg(D + c * S + d)),
-                           fmaxf(fmaxf(__ldg(D + a * S + c), __ldg(D + a * S + d)),
-                                 fmaxf(__ldg(D + b * S + c), __ldg(D + b * S + d))));
-    keep = qq * dm >= f.tolf_lo;
+  const float qb = __ldg(g.Q + bp);
+  const int gb = __ldg(ql.gbra + ib);
+  const float* D = f.Dsh + g.mol_sbase[mol];
+  const int S = g.mol_ns[mol];
+  const int a = __ldg(g.sh_local + sa), b = __ldg(g.sh_local + sb);
+  const float dab = 4.0f * __ldg(D + a * S + b);
+  const int k0 = __ldg(cl.kmoff + mol);
+  int k1 = __ldg(cl.kmoff + mol + 1);
+  if (cl.same) k1 = min(k1, ib + 1);
+  for (int base = k0; base < k1; base += kThreads) {
+    const int jk = base + threadIdx.x;
+    bool keep = jk < k1;
+    float qq = 0.f;
+    int key = 0;
+    if (keep) {
+      const int kp = __ldg(cl.ket + jk);
+      const int sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
+      qq = qb * __ldg(g.Q + kp);
+      const int c = __ldg(g.sh_local + sc), d = __ldg(g.sh_local + sd);
+      const float dm = fmaxf(fmaxf(dab, 4.0f * __ldg(D + c * S + d)),
+                             fmaxf(fmaxf(__ldg(D + a * S + c), __ldg(D + a * S + d)),
+                                   fmaxf(__ldg(D + b * S + c), __ldg(D + b * S + d))));
+      keep = qq * dm >= f.tolf_lo;
+      key = gb * ql.nkg + __ldg(ql.gket + jk);
+    }
+    const bool lo = qq < cl.qmax;  // qmax carries the FP32 split (0: none)
+    const int2 v = make_int2(ib, jk);
+    bucket_append(keep && !lo, key, v, ql.q64, ql.n64, ql.key_off);
+    if (ql.q32) bucket_append(keep && lo, key, v, ql.q32, ql.n32, ql.key_off);
   }
-  const bool lo = qq < cl.qmax;  // qmax carries the FP32 split (0: none)
-  const int key = __ldg(ql.gbra + ib) * ql.nkg + __ldg(ql.gket + jk);
-  const int2 v = make_int2(ib, jk);
-  bucket_append(keep && !lo, key, v, ql.q64, ql.n64, ql.key_off);
-  if (ql.q32) bucket_append(keep && lo, key, v, ql.q32, ql.n32, ql.key_off);
 }
 
 constexpr int kMaxKeys = 256;
@@ -199,12 +214,14 @@ constexpr size_t smem_bytes() {
 
 namespace mmdg {
 // blocks of a persistent launch: every SM filled to the kernel's occupancy
+// (grid > 0: an autotuned grid, capped at that occupancy)
 template <typename K>
-inline int persistent_blocks(K kernel, size_t smem) {
+inline int persistent_blocks(K kernel, size_t smem, int grid = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, smem);
-  return sms * (per > 0 ? per : 1);
+  const int full = sms * (per > 0 ? per : 1);
+  return grid > 0 && grid < full ? grid : full;
 }
 }  // namespace mmdg

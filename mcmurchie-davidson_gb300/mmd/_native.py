@@ -42,6 +42,10 @@ def _bind(L):
         "mmdg_boys": (c_int, [p, c_int, c_ll, p, p, p]),
         "mmdg_fock_update": (c_int, [p, p, p, p, p]),
         "mmdg_jk_dense": (c_int, [p, c_ll, p, p, p, p, p]),
+        "mmdg_one_electron": (c_int, [p, c_int, p, p, p, p, p, p, p, p, p]),
+        "mmdg_set_tuning": (c_int, [p, c_int, c_int]),
+        "mmdg_set_streams": (c_int, [p, c_int]),
+        "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,0 +1,109 @@
+"""Autotuner of the Fock-build launch schedule.
+
+Tunables (C ABI ``mmdg_set_tuning`` / ``mmdg_set_streams``):
+
+* per angular class, the persistent grid of its evaluation kernel: one full wave at
+  the kernel's occupancy (0), or k blocks per SM for k in {1, 2, 4} -- small grids
+  pack the tail of small classes, full waves hide latency in large ones;
+* the number of concurrent streams the 21 class kernels are spread over (1, 2, 4):
+  small batches leave the GPU half empty with one class at a time.
+
+Each candidate is timed with CUDA events on a representative density difference
+(``mmdg_fock_timed`` per class for the grids, whole builds for the streams).
+Results are cached as JSON under ``_build/tuning.json`` keyed by the GPU name and
+the basis signature (molecules, functions, shells).
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+import numpy as np
+
+from . import _native
+
+CACHE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "_build", "tuning.json")
+
+
+class Tuning:
+    def __init__(self, grids=None, streams=1, measured=None):
+        self.grids = list(grids) if grids is not None else [0] * _native.NCLASS
+        self.streams = int(streams)
+        self.measured = measured or {}
+
+    def apply(self, ctx):
+        for c, g in enumerate(self.grids):
+            _native.check(_native.lib().mmdg_set_tuning(ctx._h, c, int(g)), "mmdg_set_tuning")
+        _native.check(_native.lib().mmdg_set_streams(ctx._h, self.streams), "mmdg_set_streams")
+
+    def to_json(self):
+        return {"grids": self.grids, "streams": self.streams, "measured": self.measured}
+
+
+def _key(ctx):
+    torch = ctx.torch
+    name = torch.cuda.get_device_name(ctx.device)
+    return f"{name}|nmol={ctx.nmol}|nfunc={int(np.sum(ctx.nfunc))}|nshell={ctx.nshell}"
+
+
+def _time_build(ctx, dP, tol, split, reps):
+    torch = ctx.torch
+    G = torch.empty_like(dP)
+    ctx.fock(dP, G, tol=tol, fp32_below=split)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.fock(dP, G, tol=tol, fp32_below=split)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps
+
+
+def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuning:
+    key = _key(ctx)
+    cache = {}
+    if use_cache and os.path.exists(CACHE):
+        try:
+            cache = json.load(open(CACHE))
+        except (OSError, ValueError):
+            cache = {}
+        if key in cache:
+            t = cache[key]
+            tun = Tuning(t["grids"], t["streams"], t.get("measured"))
+            tun.apply(ctx)
+            return tun
+    torch = ctx.torch
+    sms = torch.cuda.get_device_properties(ctx.device).multi_processor_count
+    candidates = [0, sms, 2 * sms, 4 * sms]
+    best = np.full(_native.NCLASS, np.inf)
+    grids = [0] * _native.NCLASS
+    per = {}
+    for g in candidates:
+        Tuning([g] * _native.NCLASS, 1).apply(ctx)
+        ctx.fock_timed(dP, tol=tol, fp32_below=fp32_below)  # warm
+        acc = np.zeros(_native.NCLASS)
+        for _ in range(reps):
+            _, ms, _ = ctx.fock_timed(dP, tol=tol, fp32_below=fp32_below)
+            acc += ms
+        acc /= reps
+        per[str(g)] = acc.tolist()
+        for c in range(_native.NCLASS):
+            if acc[c] < best[c] * 0.98:  # prefer the default unless clearly better
+                best[c] = acc[c]
+                grids[c] = g
+    stream_ms = {}
+    best_s, best_t = 1, np.inf
+    for s in (1, 2, 4):
+        Tuning(grids, s).apply(ctx)
+        t = _time_build(ctx, dP, tol, fp32_below, reps)
+        stream_ms[str(s)] = t * 1e3
+        if t < best_t * 0.98:
+            best_s, best_t = s, t
+    tun = Tuning(grids, best_s, {"class_ms_by_grid": per, "build_ms_by_streams": stream_ms})
+    tun.apply(ctx)
+    if use_cache:
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        cache[key] = tun.to_json()
+        with open(CACHE, "w") as f:
+            json.dump(cache, f, indent=1)
+    return tun
