@@ -48,6 +48,10 @@ WORKLOAD = {"workload": "(H2O)16 6-31G** direct RHF", "n_water": 16, "lattice": 
 # the same rule and prints its own figure as config.fq_per_build).  Used by the
 # reference arm, which cannot run the 400-function SCF itself.
 FQ_PER_BUILD = 198282802.0
+# DRAM bytes (read + write) of one launch of the top class kernels in the first, full
+# Fock build of this workload, from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum; summary and command in profiles/k_fock_fp64_pipe_h2o16.md).
+DRAM_BYTES_PER_LAUNCH = {"1000": 48.3e6, "0000": 24.2e6, "1010": 25.6e6, "1110": 16.2e6, "2111": 5.5e6}
 
 
 def _env():
@@ -354,8 +358,10 @@ def gpu_arm(args):
     build_ms = float(class_ms.sum()) / builds
     step_other_ms = 1e3 * t_dev / builds - build_ms
     all_achieved = float(cls_flops.sum()) / (float(class_ms.sum()) / 1e3) / 1e12
+    traffic = DRAM_BYTES_PER_LAUNCH.get("%d%d%d%d" % dom_cls) if WORKLOAD["n_water"] == 16 else None
     roofline = {"bound": "fp64", "kernel": "k_fock<MD_%d%d%d%d,double>" % dom_cls, "achieved": achieved,
-                "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": traffic,
+                "traffic_note": "DRAM bytes of one iteration-1 launch (ncu); the kernel is FP64-pipe bound",
                 "peak_source": "live DFMA probe mmdg_measure_peaks (MEASURED_PEAKS.json has no FP64 figure)",
                 "flops_per_launch": float(cls_flops[dom]) / builds, "launch_ms": float(class_ms[dom]) / builds,
                 "all_classes": {"achieved": all_achieved, "frac": all_achieved / fp64_peak,
