@@ -136,6 +136,31 @@ int mmdg_set_streams(mmdg_context* ctx, int nstreams);
  * launch serves every molecule of the batch. */
 int mmdg_fock_graph(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below, void* stream);
 
+/*
+ * Learned initial guess: kernels of the density-block MLP (no counterpart in the
+ * reference, which starts every SCF from P = 0, mmd/scf.py:15,23-24).  BF16 weights,
+ * FP32 activations and accumulation; all pointers are device pointers.
+ *   mmdg_mlp_gemm      C[M,N] = op(A) op(B) + beta C; op transposes when ta/tb != 0
+ *                      (A stored K x M / B stored N x K); a_bf16 / b_bf16 mark a
+ *                      BF16 operand (at most one)
+ *   mmdg_mlp_bias_act  Z += b (per column), Y = silu(Z) (silu != 0) or Y = Z
+ *   mmdg_mlp_act_grad  dZ = dY * silu'(Z) (or dY)
+ *   mmdg_mlp_colsum    db[c] = sum_r dZ[r, c]
+ *   mmdg_mlp_mse       dY = 2 (Y - T) mask / count; *loss += sum ((Y - T) mask)^2 / count
+ *   mmdg_mlp_adam      Adam step on FP32 master weights, refreshing their BF16 copy
+ *   mmdg_mlp_to_bf16   BF16 copy of FP32 weights
+ */
+int mmdg_mlp_gemm(int M, int N, int K, const void* A, int lda, int ta, int a_bf16, const void* B, int ldb, int tb,
+                  int b_bf16, float* C, int ldc, float beta, void* stream);
+int mmdg_mlp_bias_act(float* Z, float* Y, const float* b, long long rows, int cols, int silu, void* stream);
+int mmdg_mlp_act_grad(const float* Z, const float* dY, float* dZ, long long n, int silu, void* stream);
+int mmdg_mlp_colsum(const float* dZ, float* db, long long rows, int cols, void* stream);
+int mmdg_mlp_mse(const float* Y, const float* T, const float* mask, float* dY, double* loss, long long n,
+                 float inv_count, void* stream);
+int mmdg_mlp_adam(float* w, void* w_bf16, const float* g, float* m, float* v, long long n, float lr, float b1,
+                  float b2, float eps, int step, void* stream);
+int mmdg_mlp_to_bf16(const float* w, void* w_bf16, long long n, void* stream);
+
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
 

@@ -147,14 +147,33 @@ class BatchRHF:
         Cocc = C * mask[:, None, :]
         return Cocc @ Cocc.transpose(1, 2)
 
-    def run(self, conver=1e-8, maxiter=100, DIIS=True):
-        """RHF of every molecule; returns the energies (numpy, Eh)."""
+    def run(self, conver=1e-8, maxiter=100, DIIS=True, guess=None, guess_fallback=True):
+        """RHF of every molecule; returns the energies (numpy, Eh).
+
+        ``guess``: optional list of initial densities (N_m x N_m); the first Fock
+        matrix is then Core + sym(G(P_guess)), and a molecule whose DIIS error grows
+        three iterations in a row restarts from the core guess (its stale DIIS
+        entries get zero weight)."""
         torch = self.torch
         B, Nm = self.B, self.Nmax
         X, S, Core = self.X, self.S, self.Core
         P_old = torch.zeros((B, Nm, Nm), dtype=torch.float64, device=self.dev)
         P = P_old.clone()
         F = Core.clone()
+        self.reverted = np.zeros(B, dtype=bool)
+        if guess is not None:
+            Pg = np.zeros((B, Nm, Nm))
+            for b, g in enumerate(guess):
+                n = self.N[b]
+                Pg[b, :n, :n] = g
+            P = torch.as_tensor(Pg, device=self.dev)
+            P_old = P.clone()
+            G = self._pad(self.fock(P))
+            F = Core + 0.5 * (G + G.transpose(1, 2))
+        valid_from = np.zeros(B, dtype=int)  # first usable DIIS slot (by global step) per molecule
+        revert = None
+        err_hist = []
+        hist_steps = []
         hist_F, hist_E = [], []
         done = np.zeros(B, dtype=bool)
         energy = np.zeros(B)
@@ -175,14 +194,36 @@ class BatchRHF:
                     err = X @ (FPS - FPS.transpose(1, 2)) @ X
                     hist_F.append(F)
                     hist_E.append(err)
+                    hist_steps.append(step)
                     if len(hist_F) > 8:
                         hist_F.pop(0)
                         hist_E.pop(0)
+                        hist_steps.pop(0)
                     n = len(hist_F)
                     Ev = torch.stack(hist_E, 1).reshape(B, n, -1)
                     Bm = torch.full((B, n + 1, n + 1), -1.0, dtype=torch.float64, device=self.dev)
                     Bm[:, :n, :n] = Ev @ Ev.transpose(1, 2)
                     Bm[:, n, n] = 0.0
+                    # slots from before a molecule's restart: decoupled, huge diagonal -> zero weight
+                    stale = torch.as_tensor(np.array(hist_steps)[None, :] < valid_from[:, None], device=self.dev)
+                    if bool(stale.any()):
+                        sf = stale.to(Bm.dtype)
+                        keep = 1.0 - sf
+                        Bm[:, :n, :n] = Bm[:, :n, :n] * keep[:, :, None] * keep[:, None, :]
+                        Bm[:, :n, :n] += torch.diag_embed(sf * 1e30)
+                    if guess is not None and guess_fallback:
+                        en = torch.linalg.norm(err.reshape(B, -1), dim=1).cpu().numpy()
+                        err_hist.append(en)
+                        if len(err_hist) >= 4:
+                            h4 = np.array(err_hist[-4:])
+                            grow = (h4[3] > h4[2]) & (h4[2] > h4[1]) & (h4[1] > h4[0]) & ~self.reverted & ~done
+                            if grow.any():
+                                idx = np.flatnonzero(grow)
+                                self.reverted[idx] = True
+                                valid_from[idx] = step + 1
+                                rm = torch.zeros(B, dtype=torch.bool, device=self.dev)
+                                rm[torch.as_tensor(idx, device=self.dev)] = True
+                                revert = rm[:, None, None]
                     rhs = torch.zeros((B, n + 1), dtype=torch.float64, device=self.dev)
                     rhs[:, n] = -1.0
                     # converged (frozen) molecules: a well-posed dummy system
@@ -191,6 +232,11 @@ class BatchRHF:
                     w = torch.linalg.solve(Bm, rhs)
                     Fd = torch.einsum("bi,bijk->bjk", w[:, :n], torch.stack(hist_F, 1))
                     FO = X.transpose(1, 2) @ Fd @ X
+                    if revert is not None:  # restart from the core guess: F = Core, P_old = 0
+                        F = torch.where(revert, Core, F)
+                        P_old = torch.where(revert, torch.zeros_like(P_old), P_old)
+                        FO = torch.where(revert, X.transpose(1, 2) @ Core @ X, FO)
+                        revert = None
                 else:
                     FO = X.transpose(1, 2) @ F @ X
             else:

@@ -1,0 +1,315 @@
+"""Learned initial density guess for RHF on water clusters in 6-31G.
+
+The reference starts every SCF from P = 0, i.e. F = Core (mmd/scf.py:15,23-24).
+Here a small network predicts the converged density matrix block by block from
+atom-pair features, and ``Molecule.RHF(guess=P)`` starts from it (one full Fock
+build of the guess), falling back to the core guess if the DIIS error grows for
+three consecutive iterations.
+
+Features of an ordered atom pair (A, B), A <= B, within 8 Angstrom (53 numbers):
+
+* pair type one-hot (6): O-O, O-H, H-O, H-H, O self block, H self block;
+* the distance expanded on 32 Gaussians centred 0.5 .. 8 Angstrom (width 0.24 A);
+* the direction of B in A's local frame and of A in B's (3 + 3);
+* the rotation between the two local frames, R_A R_B^T (9).
+
+An atom's local frame is built from its two nearest atoms (first axis to the
+nearest, second from the next one, third their cross product), so features and
+predictions rotate with the molecule.  The target is the density block in the two
+local frames, T_A P[A,B] T_B^T, where T rotates the p triplets and leaves s
+functions alone; it is padded to 9 x 9 (O has 9 functions in 6-31G, H has 2) with
+a mask.
+
+The network: 53 -> 256 -> 256 -> 81, SiLU, BF16 weights with FP32 accumulation,
+trained with Adam on the GPU by the kernels of csrc/mlp.cu (``mmdg_mlp_*``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _native
+
+ANG = 0.52917721092
+NIN, NHID, NOUT = 53, 256, 81
+NFUNC = {8: 9, 1: 2}           # 6-31G Cartesian functions per element
+PTRIPLETS = {8: (2, 6), 1: ()}  # first index of each p triplet in the atom's functions
+TYPES = {(8, 8): 0, (8, 1): 1, (1, 8): 2, (1, 1): 3}
+RBF_CENTERS = np.linspace(0.5, 8.0, 32) / ANG
+RBF_WIDTH = 0.24 / ANG
+CUTOFF = 8.0 / ANG
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_mlp_631g.npz")
+
+
+# ---------------------------------------------------------------- geometry
+def atom_frames(coords: np.ndarray) -> np.ndarray:
+    n = len(coords)
+    R = np.tile(np.eye(3), (n, 1, 1))
+    if n < 2:
+        return R
+    d = np.linalg.norm(coords[:, None] - coords[None], axis=-1)
+    d[np.diag_indices(n)] = np.inf
+    order = np.argsort(d, axis=1)
+    for a in range(n):
+        e1 = coords[order[a, 0]] - coords[a]
+        e1 /= np.linalg.norm(e1)
+        if n > 2:
+            v = coords[order[a, 1]] - coords[a]
+        else:
+            v = np.array([0.0, 0.0, 1.0]) if abs(e1[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+        e2 = v - np.dot(v, e1) * e1
+        nr = np.linalg.norm(e2)
+        if nr < 1e-8:
+            v = np.array([0.0, 0.0, 1.0]) if abs(e1[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+            e2 = v - np.dot(v, e1) * e1
+            nr = np.linalg.norm(e2)
+        e2 /= nr
+        R[a] = np.stack([e1, e2, np.cross(e1, e2)])
+    return R
+
+
+def block_transform(Z: int, R: np.ndarray) -> np.ndarray:
+    T = np.eye(NFUNC[Z])
+    for p in PTRIPLETS[Z]:
+        T[p:p + 3, p:p + 3] = R
+    return T
+
+
+def molecule_layout(mol):
+    """Atomic numbers, coordinates (bohr) and first-function offsets of a Molecule."""
+    Z = np.array([a.charge for a in mol.atoms])
+    X = np.array([a.origin for a in mol.atoms])
+    off = np.concatenate([[0], np.cumsum([NFUNC[int(z)] for z in Z])[:-1]])
+    if off[-1] + NFUNC[int(Z[-1])] != mol.nbasis:
+        raise ValueError("the learned guess covers H and O in 6-31G only")
+    return Z, X, off
+
+
+def pair_features(Z, X, R):
+    """Ordered pairs (A <= B) within the cutoff and their feature rows."""
+    n = len(Z)
+    pairs, rows = [], []
+    for a in range(n):
+        for b in range(a, n):
+            v = X[b] - X[a]
+            d = float(np.linalg.norm(v))
+            if d > CUTOFF:
+                continue
+            f = np.zeros(NIN)
+            if a == b:
+                f[4 if Z[a] == 8 else 5] = 1.0
+            else:
+                f[TYPES[(int(Z[a]), int(Z[b]))]] = 1.0
+                f[38:41] = R[a] @ (v / d)
+                f[41:44] = R[b] @ (-v / d)
+            f[6:38] = np.exp(-((d - RBF_CENTERS) / RBF_WIDTH) ** 2)
+            f[44:53] = (R[a] @ R[b].T).ravel()
+            pairs.append((a, b))
+            rows.append(f)
+    return pairs, np.array(rows, dtype=np.float32)
+
+
+def pair_targets(P, Z, R, off, pairs):
+    Y = np.zeros((len(pairs), NOUT), dtype=np.float32)
+    M = np.zeros((len(pairs), NOUT), dtype=np.float32)
+    for k, (a, b) in enumerate(pairs):
+        na, nb = NFUNC[int(Z[a])], NFUNC[int(Z[b])]
+        blk = P[off[a]:off[a] + na, off[b]:off[b] + nb]
+        loc = block_transform(int(Z[a]), R[a]) @ blk @ block_transform(int(Z[b]), R[b]).T
+        t = np.zeros((9, 9))
+        m = np.zeros((9, 9))
+        t[:na, :nb] = loc
+        m[:na, :nb] = 1.0
+        Y[k] = t.ravel()
+        M[k] = m.ravel()
+    return Y, M
+
+
+def assemble(pred, Z, R, off, pairs, N):
+    P = np.zeros((N, N))
+    for k, (a, b) in enumerate(pairs):
+        na, nb = NFUNC[int(Z[a])], NFUNC[int(Z[b])]
+        loc = pred[k].reshape(9, 9)[:na, :nb]
+        blk = block_transform(int(Z[a]), R[a]).T @ loc @ block_transform(int(Z[b]), R[b])
+        if a == b:
+            blk = 0.5 * (blk + blk.T)
+        P[off[a]:off[a] + na, off[b]:off[b] + nb] = blk
+        if a != b:
+            P[off[b]:off[b] + nb, off[a]:off[a] + na] = blk.T
+    return P
+
+
+def molecule_samples(mol, P=None):
+    Z, X, off = molecule_layout(mol)
+    R = atom_frames(X)
+    pairs, F = pair_features(Z, X, R)
+    if P is None:
+        return pairs, F, None, None, (Z, R, off)
+    Y, M = pair_targets(np.asarray(P), Z, R, off, pairs)
+    return pairs, F, Y, M, (Z, R, off)
+
+
+# ---------------------------------------------------------------- the network
+class DensityMLP:
+    """53 -> 256 -> 256 -> 81 MLP; FP32 master weights, BF16 copies used by the kernels."""
+
+    def __init__(self, seed=0, weights=None):
+        torch = _native._torch()
+        self.torch = torch
+        self.dev = "cuda"
+        _native.lib()
+        L = _native.lib()
+        self._sig(L)
+        rng = np.random.default_rng(seed)
+        shapes = [(NHID, NIN), (NHID, NHID), (NOUT, NHID)]
+        if weights is None:
+            W = [rng.standard_normal(s) * np.sqrt(1.0 / s[1]) for s in shapes]
+            b = [np.zeros(s[0]) for s in shapes]
+        else:
+            W = [weights[f"W{i}"] for i in range(3)]
+            b = [weights[f"b{i}"] for i in range(3)]
+        f32 = lambda a: torch.tensor(np.asarray(a, dtype=np.float32), device=self.dev)
+        self.W = [f32(w).contiguous() for w in W]
+        self.b = [f32(x).contiguous() for x in b]
+        self.Wb = [torch.empty(w.shape, dtype=torch.bfloat16, device=self.dev) for w in self.W]
+        for w, wb in zip(self.W, self.Wb):
+            _native.check(L.mmdg_mlp_to_bf16(self._p(w), self._p(wb), w.numel(), _native.stream_ptr()), "to_bf16")
+        self.mW = [torch.zeros_like(w) for w in self.W]
+        self.vW = [torch.zeros_like(w) for w in self.W]
+        self.mb = [torch.zeros_like(x) for x in self.b]
+        self.vb = [torch.zeros_like(x) for x in self.b]
+        self.step = 0
+
+    @staticmethod
+    def _sig(L):
+        p, c_int, c_ll, c_f = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_float
+        for name, args in {
+            "mmdg_mlp_gemm": [c_int, c_int, c_int, p, c_int, c_int, c_int, p, c_int, c_int, c_int, p, c_int, c_f, p],
+            "mmdg_mlp_bias_act": [p, p, p, c_ll, c_int, c_int, p],
+            "mmdg_mlp_act_grad": [p, p, p, c_ll, c_int, p],
+            "mmdg_mlp_colsum": [p, p, c_ll, c_int, p],
+            "mmdg_mlp_mse": [p, p, p, p, p, c_ll, c_f, p],
+            "mmdg_mlp_adam": [p, p, p, p, p, c_ll, c_f, c_f, c_f, c_f, c_int, p],
+            "mmdg_mlp_to_bf16": [p, p, c_ll, p],
+        }.items():
+            fn = getattr(L, name)
+            fn.restype = ctypes.c_int
+            fn.argtypes = args
+
+    @staticmethod
+    def _p(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def forward(self, X):
+        """X: (B, 53) float32 CUDA tensor -> list of (Z, Y) per layer (Y of the last = output)."""
+        torch, L, st = self.torch, _native.lib(), _native.stream_ptr()
+        acts = []
+        h = X
+        for i in range(3):
+            out = self.W[i].shape[0]
+            Zt = torch.empty((h.shape[0], out), dtype=torch.float32, device=self.dev)
+            _native.check(L.mmdg_mlp_gemm(h.shape[0], out, h.shape[1], self._p(h), h.shape[1], 0, 0,
+                                          self._p(self.Wb[i]), h.shape[1], 1, 1, self._p(Zt), out, 0.0, st), "gemm")
+            Yt = torch.empty_like(Zt)
+            _native.check(L.mmdg_mlp_bias_act(self._p(Zt), self._p(Yt), self._p(self.b[i]), h.shape[0], out,
+                                              1 if i < 2 else 0, st), "bias_act")
+            acts.append((h, Zt, Yt))
+            h = Yt
+        return acts
+
+    def predict(self, X):
+        return self.forward(X)[-1][2]
+
+    def backward(self, acts, dY):
+        """Gradients (dW, db) of every layer from the output gradient dY."""
+        torch, L, st = self.torch, _native.lib(), _native.stream_ptr()
+        grads = [None] * 3
+        d = dY
+        for i in (2, 1, 0):
+            h, Zt, _ = acts[i]
+            out, inp = self.W[i].shape
+            dZ = torch.empty_like(Zt)
+            _native.check(L.mmdg_mlp_act_grad(self._p(Zt), self._p(d), self._p(dZ), dZ.numel(), 1 if i < 2 else 0, st),
+                          "act_grad")
+            dW = torch.empty((out, inp), dtype=torch.float32, device=self.dev)
+            _native.check(L.mmdg_mlp_gemm(out, inp, h.shape[0], self._p(dZ), out, 1, 0, self._p(h), inp, 0, 0,
+                                          self._p(dW), inp, 0.0, st), "gemm dW")
+            db = torch.empty(out, dtype=torch.float32, device=self.dev)
+            _native.check(L.mmdg_mlp_colsum(self._p(dZ), self._p(db), h.shape[0], out, st), "colsum")
+            grads[i] = (dW, db)
+            if i > 0:
+                dh = torch.empty((h.shape[0], inp), dtype=torch.float32, device=self.dev)
+                _native.check(L.mmdg_mlp_gemm(h.shape[0], inp, out, self._p(dZ), out, 0, 0, self._p(self.Wb[i]), inp,
+                                              0, 1, self._p(dh), inp, 0.0, st), "gemm dX")
+                d = dh
+        return grads
+
+    def loss_grad(self, Y, T, M):
+        torch, L, st = self.torch, _native.lib(), _native.stream_ptr()
+        dY = torch.empty_like(Y)
+        loss = torch.zeros(1, dtype=torch.float64, device=self.dev)
+        cnt = float(max(M.sum().item(), 1.0))
+        _native.check(L.mmdg_mlp_mse(self._p(Y), self._p(T), self._p(M), self._p(dY), self._p(loss), Y.numel(),
+                                     1.0 / cnt, st), "mse")
+        return loss, dY
+
+    def adam(self, grads, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        L, st = _native.lib(), _native.stream_ptr()
+        self.step += 1
+        for i, (dW, db) in enumerate(grads):
+            _native.check(L.mmdg_mlp_adam(self._p(self.W[i]), self._p(self.Wb[i]), self._p(dW), self._p(self.mW[i]),
+                                          self._p(self.vW[i]), dW.numel(), lr, b1, b2, eps, self.step, st), "adam W")
+            _native.check(L.mmdg_mlp_adam(self._p(self.b[i]), None, self._p(db), self._p(self.mb[i]),
+                                          self._p(self.vb[i]), db.numel(), lr, b1, b2, eps, self.step, st), "adam b")
+
+    def state(self):
+        out = {}
+        for i in range(3):
+            out[f"W{i}"] = self.W[i].cpu().numpy()
+            out[f"b{i}"] = self.b[i].cpu().numpy()
+        return out
+
+    def save(self, path=WEIGHTS):
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        np.savez_compressed(path, **self.state())
+
+    @classmethod
+    def load(cls, path=WEIGHTS):
+        return cls(weights=dict(np.load(path)))
+
+
+def train(features, targets, masks, epochs=30, batch=8192, lr=2e-3, seed=0, log=None):
+    """Adam on masked MSE; features/targets/masks are float32 arrays (rows = pairs)."""
+    net = DensityMLP(seed=seed)
+    torch = net.torch
+    Xd = torch.tensor(features, device="cuda")
+    Yd = torch.tensor(targets, device="cuda")
+    Md = torch.tensor(masks, device="cuda")
+    n = Xd.shape[0]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    history = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, device="cuda", generator=g)
+        lr_ep = lr * 0.5 * (1 + np.cos(np.pi * ep / epochs))
+        tot = 0.0
+        for s in range(0, n, batch):
+            idx = perm[s:s + batch]
+            X, T, M = Xd[idx].contiguous(), Yd[idx].contiguous(), Md[idx].contiguous()
+            acts = net.forward(X)
+            loss, dY = net.loss_grad(acts[-1][2], T, M)
+            net.adam(net.backward(acts, dY), lr=lr_ep)
+            tot += float(loss.item()) * X.shape[0]
+        history.append(tot / n)
+        if log:
+            log(f"epoch {ep}: loss {tot / n:.3e}")
+    net.history = history
+    return net
+
+
+def predict_density(net, mol):
+    pairs, F, _, _, (Z, R, off) = molecule_samples(mol)
+    pred = net.predict(net.torch.tensor(F, device="cuda")).cpu().numpy()
+    return assemble(pred, Z, R, off, pairs, mol.nbasis)

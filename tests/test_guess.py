@@ -1,0 +1,112 @@
+"""Learned initial guess: host-side geometry logic (CPU) and the GPU MLP kernels'
+gradients against the CPU oracle; the trained network's gain over the core guess."""
+import os
+
+import numpy as np
+import pytest
+
+
+def _water_mol(n=3, seed=7):
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    return Molecule(water_cluster(n, seed=seed), "6-31g")
+
+
+def _rotated(mol, R):
+    from mmd.molecule import Molecule
+    lines = [f"{0} {1}"]
+    for a in mol.atoms:
+        x = R @ (a.origin * 0.52917721092)
+        lines.append(f"{'O' if a.charge == 8 else 'H'} {x[0]:.12f} {x[1]:.12f} {x[2]:.12f}")
+    return Molecule("\n" + "\n".join(lines) + "\n", "6-31g")
+
+
+def test_pair_features_are_rotation_invariant():
+    from mmd import guess as G
+    from mmd.clusters import random_rotation
+    m = _water_mol()
+    R = random_rotation(np.random.default_rng(1))
+    p1, f1, _, _, _ = G.molecule_samples(m)
+    p2, f2, _, _, _ = G.molecule_samples(_rotated(m, R))
+    assert p1 == p2
+    assert np.abs(f1 - f2).max() < 1e-5
+
+
+def test_block_targets_round_trip():
+    """targets (local frames) -> assemble (lab frame) reproduces every block within the cutoff."""
+    from mmd import guess as G
+    m = _water_mol(2)
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((m.nbasis, m.nbasis))
+    P = A + A.T
+    pairs, F, Y, M, (Z, R, off) = G.molecule_samples(m, P)
+    Pa = G.assemble(Y, Z, R, off, pairs, m.nbasis)
+    assert np.abs(Pa - P).max() < 1e-5  # float32 targets; both waters are within 8 Angstrom
+
+
+def test_rotated_targets_are_invariant():
+    from mmd import guess as G
+    from mmd.clusters import random_rotation
+    m = _water_mol(2, seed=5)
+    R = random_rotation(np.random.default_rng(3))
+    # density of the rotated molecule = the rotated density (p blocks rotate, s do not)
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((m.nbasis, m.nbasis))
+    P = A + A.T
+    Z, X, off = G.molecule_layout(m)
+    T = np.zeros((m.nbasis, m.nbasis))
+    for a, z in enumerate(Z):
+        n = G.NFUNC[int(z)]
+        T[off[a]:off[a] + n, off[a]:off[a] + n] = G.block_transform(int(z), R)
+    Prot = T @ P @ T.T
+    _, _, Y1, _, _ = G.molecule_samples(m, P)
+    _, _, Y2, _, _ = G.molecule_samples(_rotated(m, R), Prot)
+    assert np.abs(Y1 - Y2).max() < 1e-4
+
+
+@pytest.mark.gpu
+def test_mlp_kernels_gradients_match_cpu_oracle():
+    import torch
+    import mlp_oracle as O
+    from mmd import guess as G
+    net = G.DensityMLP(seed=3)
+    rng = np.random.default_rng(9)
+    B = 300
+    X = rng.standard_normal((B, G.NIN)).astype(np.float32)
+    T = rng.standard_normal((B, G.NOUT)).astype(np.float32)
+    M = (rng.random((B, G.NOUT)) < 0.6).astype(np.float32)
+    # the oracle uses the same BF16-rounded weights the kernels read
+    W = [w.float().cpu().numpy().astype(np.float64) for w in net.Wb]
+    b = [x.cpu().numpy().astype(np.float64) for x in net.b]
+    loss_o, grads_o = O.loss_and_grads(W, b, X.astype(np.float64), T.astype(np.float64), M.astype(np.float64))
+    acts = net.forward(torch.tensor(X, device="cuda"))
+    loss, dY = net.loss_grad(acts[-1][2], torch.tensor(T, device="cuda"), torch.tensor(M, device="cuda"))
+    grads = net.backward(acts, dY)
+    assert abs(loss.item() - loss_o) < 1e-4 * abs(loss_o)
+    Y_o = O.forward(W, b, X.astype(np.float64))[-1][2]
+    assert np.abs(acts[-1][2].cpu().numpy() - Y_o).max() < 1e-4 * np.abs(Y_o).max()
+    for (dW, db), (dWo, dbo) in zip(grads, grads_o):
+        assert np.abs(dW.cpu().numpy() - dWo).max() < 2e-3 * np.abs(dWo).max()
+        assert np.abs(db.cpu().numpy() - dbo).max() < 2e-3 * np.abs(dbo).max()
+
+
+@pytest.mark.gpu
+def test_learned_guess_gains_over_core_guess():
+    """The committed network (trained by mmd.guess_train on 20k clusters) cuts the SCF
+    iterations of held-out (H2O)8 clusters; energies agree with the core-guess SCF."""
+    from mmd import guess as G
+    from mmd.batch import BatchRHF
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    if not os.path.exists(G.WEIGHTS):
+        pytest.skip("network not trained yet")
+    net = G.DensityMLP.load()
+    geoms = [water_cluster(8, seed=900000 + k) for k in range(8)]
+    gs = [G.predict_density(net, Molecule(g, "6-31g")) for g in geoms]
+    core = BatchRHF(geoms, "6-31g")
+    Ec = core.run(conver=1e-9)
+    learned = BatchRHF(geoms, "6-31g")
+    El = learned.run(conver=1e-9, guess=gs)
+    assert core.converged.all() and learned.converged.all()
+    assert np.abs(El - Ec).max() < 1e-8
+    assert learned.iterations.mean() < core.iterations.mean()
