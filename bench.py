@@ -284,6 +284,124 @@ def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3):
             "mean_energy": float(np.mean(E))}
 
 
+def mixed_bench(n_water=32, thr=1e-5, conver=1e-8, seed=32):
+    """Seeded (H2O)32 (4x4x2 lattice), 6-31G**, ~800 functions: direct RHF in FP64 and
+    with quartets of Schwarz bound < thr in FP32.  Time to converge of both, and, in a
+    second (checked) pass of each, the max |F - F_ref| of every iteration's Fock matrix
+    against a from-scratch FP64 build on the same density (the FP64 pass gives the
+    floor that incremental builds at acc2e = 1e-12 reach on their own)."""
+    import numpy as np
+    import torch
+    from mmd.clusters import water_cluster
+    from mmd.integrals import twoe
+    from mmd.molecule import Molecule
+    geom = water_cluster(n_water, seed=seed)
+    out = {"workload": f"(H2O){n_water} 6-31G** direct RHF, seed {seed}", "fp32_below": thr, "conver": conver}
+    for name, fp in (("fp64", 0.0), ("mixed", thr)):
+        twoe._ctx_cache.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m = Molecule(geom, "6-31gss")
+        E = float(m.RHF(doPrint=False, direct=True, fp32_below=fp, conver=conver))
+        torch.cuda.synchronize()
+        out[name] = {"energy": E, "time_to_converge_s": time.perf_counter() - t0, "iterations": int(m.iterations),
+                     "converged": bool(m.is_converged)}
+    out["nbasis"] = int(m.nbasis)
+    out["energy_error_vs_fp64"] = out["mixed"]["energy"] - out["fp64"]["energy"]
+    out["ttc_speedup"] = out["fp64"]["time_to_converge_s"] / out["mixed"]["time_to_converge_s"]
+    for name, fp in (("fp64", 0.0), ("mixed", thr)):
+        st = m.scf_begin(direct=True, fp32_below=fp, build=False)
+        ctx, errs = m.context, []
+        for step in range(m.maxiter):
+            st.iterate()
+            if step > 0:
+                P = st.last_dP[0].contiguous()
+                G = ctx.fock(P.view(-1), tol=m.scrTol, fp32_below=0.0).view(m.nbasis, m.nbasis)
+                Fref = st.Core + 0.5 * (G + G.T)
+                errs.append(float((st.F - Fref).abs().max().item()))
+                if m.P_RMS < conver:
+                    break
+        out[name]["fock_max_error_per_iteration"] = errs
+    # one full Fock build (converged density) in each precision, CUDA-event timed
+    P = st.P.contiguous().view(-1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, fp in (("fp64", 0.0), ("mixed", thr)):
+        ctx.fock(P, tol=m.scrTol, fp32_below=fp)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(3):
+            ctx.fock(P, tol=m.scrTol, fp32_below=fp)
+        e1.record()
+        torch.cuda.synchronize()
+        out[name]["full_fock_build_ms"] = e0.elapsed_time(e1) / 3
+    out["fock_build_speedup"] = out["fp64"]["full_fock_build_ms"] / out["mixed"]["full_fock_build_ms"]
+    return out
+
+
+def _polished_energy(mol):
+    """E(P) = tr((H + F(P)) P) + E_nuc with one non-incremental FP64 Fock build of the
+    converged density of a finished Molecule(...).RHF(direct=True)."""
+    import numpy as np
+    import torch
+    ctx = mol.context
+    P = torch.as_tensor(np.ascontiguousarray(mol.P.real), device="cuda")
+    G = ctx.fock(P.reshape(-1), tol=mol.scrTol, fp32_below=0.0).view(mol.nbasis, mol.nbasis)
+    Core = mol._dev["Core"]
+    F = Core + 0.5 * (G + G.T)
+    return float(torch.sum((Core + F) * P.T).item()) + mol.nuc_energy
+
+
+def combined_bench(nmol=64, thr=1e-5, conver=1e-8):
+    """The three changes together on held-out seeded (H2O)8 clusters (6-31G): the plain
+    FP64 GPU path (one Molecule(...).RHF(direct=True) after another, core guess) vs
+    one BatchRHF over all molecules with FP32 below Schwarz thr and the learned guess
+    (energies from an FP64 polish build), with two ablations (batched FP64 core
+    guess, batched mixed core guess).  Times are wall clock from geometry strings to
+    converged energies (set-up included).  Energy errors are against the FP64
+    oracle energy of each molecule: the polished energy of the plain path's density."""
+    import numpy as np
+    import torch
+    from mmd import guess as G
+    from mmd.batch import BatchRHF
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    geoms = [water_cluster(8, seed=900000 + k) for k in range(nmol)]
+    Molecule(geoms[0], "6-31g").RHF(doPrint=False, direct=True, conver=conver)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    Ep, itp, mols = [], [], []
+    for g in geoms:
+        m = Molecule(g, "6-31g")
+        Ep.append(float(m.RHF(doPrint=False, direct=True, conver=conver)))
+        itp.append(int(m.iterations))
+        mols.append(m)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    Ep = np.array(Ep)
+    Eo = np.array([_polished_energy(m) for m in mols])
+    out = {"molecules": nmol, "workload": "(H2O)8 6-31G, seeds 900000+k (held out from training)",
+           "conver": conver, "fp32_below": thr,
+           "plain_fp64": {"time_to_converge_s": t_plain, "mean_iterations": float(np.mean(itp)),
+                          "max_abs_energy_error_vs_oracle": float(np.abs(Ep - Eo).max())}}
+    net = G.DensityMLP.load()
+    for name, fp, learned in (("batched_fp64_core", 0.0, False), ("batched_mixed_core", thr, False),
+                              ("batched_mixed_learned", thr, True)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gs = [G.predict_density(net, Molecule(g, "6-31g")) for g in geoms] if learned else None
+        br = BatchRHF(geoms, "6-31g", fp32_below=fp)
+        E = br.run(conver=conver, guess=gs, polish=True)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        out[name] = {"time_to_converge_s": t, "speedup_vs_plain": t_plain / t,
+                     "mean_iterations": float(br.iterations.mean()), "converged": int(br.converged.sum()),
+                     "max_abs_energy_error_vs_oracle": float(np.abs(E - Eo).max()),
+                     "max_abs_energy_error_vs_oracle_unpolished": float(np.abs(br.energies_raw - Eo).max())}
+        if learned:
+            out[name]["reverted_to_core"] = int(br.reverted.sum())
+    return out
+
+
 # ------------------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import numpy as np
@@ -405,12 +523,22 @@ def gpu_arm(args):
     # our kernels per Fock build: |dP| copy, shell-block maxima, one launch per class
     # (two with the FP32 split), symmetrised update
     launches_per_build = 3 + len(flop_model.CLASSES) * (2 if fp32 > 0 else 1)
-    batched = None
+    batched = mixed = combined = None
     if rank == 0 and not args.no_batch:
         try:
             batched = batched_bench()
         except Exception as e:  # reported, never required for the headline
             batched = {"error": str(e)[:300]}
+    if rank == 0 and not args.no_mixed:
+        try:
+            mixed = mixed_bench()
+        except Exception as e:
+            mixed = {"error": str(e)[:300]}
+    if rank == 0 and not args.no_combined:
+        try:
+            combined = combined_bench()
+        except Exception as e:
+            combined = {"error": str(e)[:300]}
     line = {
         "metric": "Fock builds/s ((H2O)16 6-31G** direct RHF, 20 iterations)",
         "value": value, "unit": "Fock builds/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -423,7 +551,7 @@ def gpu_arm(args):
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches_per_build * builds, "wall_s": wall,
         "step_breakdown_ms": {"fock_build_kernels": build_ms, "rest_of_step": step_other_ms},
-        "batched": batched,
+        "batched": batched, "mixed_precision": mixed, "combined_form": combined,
         "class_ms_per_build": {"%d%d%d%d" % c: float(x) / builds for c, x in zip(flop_model.CLASSES, class_ms)},
         "class_counts_per_build": {"%d%d%d%d" % c: [float(v) / builds for v in row]
                                    for c, row in zip(flop_model.CLASSES, counts)},
@@ -465,6 +593,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge run")
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-molecule batched sub-benchmark")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the (H2O)32 mixed-precision sub-benchmark")
+    ap.add_argument("--no-combined", action="store_true", help="skip the learned+batched+mixed sub-benchmark")
     ap.add_argument("--n-water", type=int, default=16, help="cluster size (16 = the benchmark workload)")
     ap.add_argument("--cpu-sample", metavar="SPEC")
     ap.add_argument("--cores", type=int, default=None)

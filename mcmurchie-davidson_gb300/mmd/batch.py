@@ -23,6 +23,7 @@ import numpy as np
 from . import _native
 from .integrals.shells import shells_from_bfs
 from .molecule import Molecule
+from .scf import diis_error_growing
 
 
 class BatchRHF:
@@ -147,8 +148,15 @@ class BatchRHF:
         Cocc = C * mask[:, None, :]
         return Cocc @ Cocc.transpose(1, 2)
 
-    def run(self, conver=1e-8, maxiter=100, DIIS=True, guess=None, guess_fallback=True):
+    def run(self, conver=1e-8, maxiter=100, DIIS=True, guess=None, guess_fallback=True, polish=False):
         """RHF of every molecule; returns the energies (numpy, Eh).
+
+        ``polish``: after convergence, one non-incremental FP64 Fock build of the
+        converged densities and the energy E(P) = tr((H + F(P)) P) + E_nuc from it
+        (returned; the SCF's own last energies stay in ``energies_raw``).  This
+        removes what the incremental builds accumulate (screening drops, FP32
+        quartets) from the energy and leaves only the density's own convergence
+        error, which enters the energy to second order.
 
         ``guess``: optional list of initial densities (N_m x N_m); the first Fock
         matrix is then Core + sym(G(P_guess)), and a molecule whose DIIS error grows
@@ -214,16 +222,14 @@ class BatchRHF:
                     if guess is not None and guess_fallback:
                         en = torch.linalg.norm(err.reshape(B, -1), dim=1).cpu().numpy()
                         err_hist.append(en)
-                        if len(err_hist) >= 4:
-                            h4 = np.array(err_hist[-4:])
-                            grow = (h4[3] > h4[2]) & (h4[2] > h4[1]) & (h4[1] > h4[0]) & ~self.reverted & ~done
-                            if grow.any():
-                                idx = np.flatnonzero(grow)
-                                self.reverted[idx] = True
-                                valid_from[idx] = step + 1
-                                rm = torch.zeros(B, dtype=torch.bool, device=self.dev)
-                                rm[torch.as_tensor(idx, device=self.dev)] = True
-                                revert = rm[:, None, None]
+                        grow = diis_error_growing(err_hist) & ~self.reverted & ~done
+                        if grow.any():
+                            idx = np.flatnonzero(grow)
+                            self.reverted[idx] = True
+                            valid_from[idx] = step + 1
+                            rm = torch.zeros(B, dtype=torch.bool, device=self.dev)
+                            rm[torch.as_tensor(idx, device=self.dev)] = True
+                            revert = rm[:, None, None]
                     rhs = torch.zeros((B, n + 1), dtype=torch.float64, device=self.dev)
                     rhs[:, n] = -1.0
                     # converged (frozen) molecules: a well-posed dummy system
@@ -257,9 +263,18 @@ class BatchRHF:
             E_old = energy
             if done.all():
                 break
-        self.energies = energy
+        self.energies_raw = energy
         self.converged = done
         self.P = P
+        if polish:
+            dP = self._pack(P)
+            G = torch.empty_like(dP)
+            self.ctx.fock(dP, G, tol=self.acc2e, fp32_below=0.0)
+            Gp = self._pad(G)
+            Fp = Core + 0.5 * (Gp + Gp.transpose(1, 2))
+            energy = (torch.sum((Core + Fp) * P.transpose(1, 2), dim=(1, 2))).cpu().numpy() + self.nuc
+            self.fock_builds += 1
+        self.energies = energy
         return energy
 
 

@@ -47,6 +47,9 @@ def dataset(mols, dens):
 
 
 def evaluate(net, geoms, log=print):
+    """Core vs learned guess on the same molecules (batched, FP64, conver 1e-8): SCF
+    iterations and wall time; then both again at conver 1e-10 with an FP64 polish
+    build (BatchRHF.run(polish=True)) for the energy comparison."""
     from .molecule import Molecule
     mols = [Molecule(g, "6-31g") for g in geoms]
     t0 = time.perf_counter()
@@ -56,20 +59,30 @@ def evaluate(net, geoms, log=print):
     for name, gs in (("core", None), ("learned", guesses)):
         br = BatchRHF(geoms, "6-31g")
         t0 = time.perf_counter()
-        E = br.run(conver=1e-8, guess=gs)
+        br.run(conver=1e-8, guess=gs)
         t = time.perf_counter() - t0
-        res[name] = {"energies": E, "iterations": br.iterations.copy(), "time_s": t,
-                     "converged": int(br.converged.sum()), "reverted": int(br.reverted.sum())}
-        log(f"  {name}: mean iterations {br.iterations.mean():.2f}, time {t:.2f} s")
+        r = {"energies": br.energies_raw.copy(), "iterations": br.iterations.copy(), "time_s": t,
+             "converged": int(br.converged.sum()), "reverted": int(br.reverted.sum())}
+        r["polished"] = br.run(conver=1e-10, guess=gs, polish=True).copy()
+        r["converged_tight"] = int(br.converged.sum())
+        res[name] = r
+        log(f"  {name}: mean iterations {r['iterations'].mean():.2f}, time {t:.2f} s")
     dE = np.abs(res["learned"]["energies"] - res["core"]["energies"])
+    dEp = np.abs(res["learned"]["polished"] - res["core"]["polished"])
     return {
         "molecules": len(geoms),
         "core_mean_iterations": float(res["core"]["iterations"].mean()),
         "learned_mean_iterations": float(res["learned"]["iterations"].mean()),
         "core_time_s": res["core"]["time_s"], "learned_time_s": res["learned"]["time_s"] + t_pred,
         "guess_prediction_s": t_pred,
-        "max_abs_energy_difference": float(dE.max()), "reverted_to_core": res["learned"]["reverted"],
+        "max_abs_energy_difference_conver_1e-8": float(dE.max()),
+        "max_abs_energy_difference_polished": float(dEp.max()),
+        "reverted_to_core": res["learned"]["reverted"],
         "converged": [res["core"]["converged"], res["learned"]["converged"]],
+        "converged_tight": [res["core"]["converged_tight"], res["learned"]["converged_tight"]],
+        "iterations_core": res["core"]["iterations"].tolist(),
+        "iterations_learned": res["learned"]["iterations"].tolist(),
+        "energies_polished_core": res["core"]["polished"].tolist(),
     }
 
 
@@ -79,12 +92,20 @@ def main(argv=None):
     ap.add_argument("--eval", type=int, default=500)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--out", default="gpurun_out")
+    ap.add_argument("--eval-only", action="store_true", help="evaluate the committed weights only")
     args = ap.parse_args(argv)
     from .molecule import Molecule
+    eval_geoms = [water_cluster(8, seed=900000 + k) for k in range(args.eval)]
+    if args.eval_only:
+        ev = evaluate(G.DensityMLP.load(), eval_geoms)
+        os.makedirs(args.out, exist_ok=True)
+        with open(os.path.join(args.out, "guess_eval.json"), "w") as f:
+            json.dump(ev, f, indent=1)
+        print(json.dumps({k: v for k, v in ev.items() if not isinstance(v, list)}))
+        return
     rng = np.random.default_rng(2025)
     sizes = rng.integers(1, 7, size=args.train)
     train_geoms = [water_cluster(int(n), seed=200000 + k) for k, n in enumerate(sizes)]
-    eval_geoms = [water_cluster(8, seed=900000 + k) for k in range(args.eval)]
     t0 = time.perf_counter()
     dens = converged_densities(train_geoms)
     t_data = time.perf_counter() - t0
@@ -102,7 +123,7 @@ def main(argv=None):
               "epochs": args.epochs, "loss_history": net.history, "evaluation": ev}
     with open(os.path.join(args.out, "guess_report.json"), "w") as f:
         json.dump(report, f, indent=1)
-    print(json.dumps(report["evaluation"]))
+    print(json.dumps({k: v for k, v in ev.items() if not isinstance(v, list)}))
 
 
 if __name__ == "__main__":

@@ -30,6 +30,18 @@ import numpy as np
 
 # dense symmetric eigensolver of the SCF: host LAPACK up to this size, cuSOLVER above
 HOST_EIGH_MAX_N = 640
+# an initial guess is abandoned (restart from the core guess) when the DIIS error
+# has grown this many iterations in a row
+GUESS_FALLBACK_GROWTH = 3
+
+
+def diis_error_growing(history, times=GUESS_FALLBACK_GROWTH):
+    """True where the last ``times`` DIIS errors each grew (history: list of scalars
+    or of equally shaped arrays, oldest first); False while the history is shorter."""
+    if len(history) < times + 1:
+        return np.zeros(np.shape(history[-1]) if history else (), dtype=bool)
+    h = np.asarray(history[-(times + 1):], dtype=float)
+    return np.all(h[1:] > h[:-1], axis=0)
 
 
 class SCF(object):
@@ -241,8 +253,7 @@ class _RHFState:
                 self.FO = X.T @ F_diis @ X
                 eh = self.err_hist
                 eh.append(derr)
-                if (mol.guess_used and self.guess_fallback and not mol.guess_reverted and len(eh) >= 4
-                        and eh[-1] > eh[-2] > eh[-3] > eh[-4]):
+                if mol.guess_used and self.guess_fallback and not mol.guess_reverted and diis_error_growing(eh):
                     # the initial guess misbehaves: restart from the core guess
                     mol.guess_reverted = True
                     self.P_old = torch.zeros_like(self.P)
