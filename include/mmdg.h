@@ -129,6 +129,24 @@ long long mmdg_boys_table(double* out, long long n);
 int mmdg_set_tuning(mmdg_context* ctx, int cls, int grid_blocks);
 int mmdg_set_streams(mmdg_context* ctx, int nstreams);
 
+/* Primitive-pair screening of the next mmdg_set_basis (no counterpart in the
+ * reference, which sums every primitive quartet, cython/twoe.pyx:36-50): a primitive
+ * pair whose Schwarz factor q = max sqrt((a_i b_j|a_i b_j)) (contraction weights
+ * included) satisfies q * q_max < tol is not stored, so no contracted ERI moves by
+ * more than (primitive quartets per shell quartet) * tol.  Default 1e-18; 0 keeps
+ * every primitive pair. */
+int mmdg_set_prim_tol(mmdg_context* ctx, double tol);
+
+/* Analytic RHF nuclear gradient dE/dR (replaces the Forces.forces loops of
+ * mmd/forces.py:8-97 with their ERIx/Sx/Tx/VxA/VxB derivative integrals,
+ * cython/grad.pyx:11-330): P and W = P F P are the converged density and
+ * energy-weighted density (device, N x N, the reference's P = C_occ C_occ^T);
+ * atom_xyz (bohr, natom x 3), atom_Z and shell_atom (the atom of every shell of the
+ * basis) are host arrays; grad (host, natom x 3) receives dE/dR including the nuclear
+ * repulsion (the reference's forces are -grad).  One molecule per context. */
+int mmdg_rhf_gradient(mmdg_context* ctx, const double* P, const double* W, int natom, const double* atom_xyz,
+                      const double* atom_Z, const int* shell_atom, double* grad, void* stream);
+
 /* mmdg_fock replayed as one CUDA graph: the first call with a given (dP, G, tol,
  * fp32_below) runs the build eagerly and captures its launches (screening, class
  * kernels over all molecules, memsets) into a graph; later calls with the same

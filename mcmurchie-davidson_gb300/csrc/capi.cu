@@ -201,6 +201,9 @@ struct mmdg_context {
   DevBuf<int> d_L, d_nprim, d_poff, d_func, d_shmol, d_shlocal;
   DevBuf<long long> d_mol_base, d_mol_sbase, d_mol_tbase;
   DevBuf<int> d_mol_n, d_mol_ns;
+  // primitive pairs whose Schwarz factor times the largest one is below prim_tol are
+  // not stored (0: keep all); set before the basis (mmdg_set_prim_tol)
+  double prim_tol = 1e-18;
   // pairs
   int npair = 0;
   long long nprimpair = 0, nE = 0;
@@ -355,65 +358,66 @@ __global__ void k_build_pairs(PairBuildArgs a) {
         for (int yb = lb - xb; yb >= 0; --yb)
           nnz += (xa + xb + 1) * (ya + yb + 1) * ((la - xa - ya) + (lb - xb - yb) + 1);
   const double AB[3] = {ABx, ABy, ABz};
-  for (int ka = 0; ka < Ka; ++ka)
-    for (int kb = 0; kb < Kb; ++kb) {
-      const int k = ka * Kb + kb;
-      const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
-      const double p = ea + eb, ip = 1.0 / p, mu = ea * eb * ip;
-      const double Px = (ea * Ax + eb * Bx) * ip, Py = (ea * Ay + eb * By) * ip, Pz = (ea * Az + eb * Bz) * ip;
-      const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * ip;
-      const long long pp = a.prb[pr] + k;
-      a.pP[pp] = make_double4_32a(p, Px, Py, Pz);
-      if (a.pPf) {
-        const float hx = float(Px), hy = float(Py), hz = float(Pz);
-        a.pPf[2 * pp] = make_float4(float(p), hx, hy, hz);
-        a.pPf[2 * pp + 1] = make_float4(0.f, float(Px - hx), float(Py - hy), float(Pz - hz));
-      }
-      // 1D tables E[d][i][j][t], i<=2, j<=2, t<=4
-      double E[3][3][3][5];
-      const double i2p = 0.5 * ip;
-      for (int d = 0; d < 3; ++d) {
-        const double XPA = -(eb * ip) * AB[d], XPB = (ea * ip) * AB[d];
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 3; ++j)
-            for (int t = 0; t < 5; ++t) E[d][i][j][t] = 0.0;
-        E[d][0][0][0] = 1.0;
-        for (int i = 0; i < la; ++i)
-          for (int t = 0; t <= i + 1; ++t) {
-            double v = XPA * E[d][i][0][t];
-            if (t > 0) v += i2p * E[d][i][0][t - 1];
-            if (t + 1 <= i) v += (t + 1) * E[d][i][0][t + 1];
-            E[d][i + 1][0][t] = v;
-          }
-        for (int j = 0; j < lb; ++j)
-          for (int i = 0; i <= la; ++i)
-            for (int t = 0; t <= i + j + 1; ++t) {
-              double v = XPB * E[d][i][j][t];
-              if (t > 0) v += i2p * E[d][i][j][t - 1];
-              if (t + 1 <= i + j) v += (t + 1) * E[d][i][j][t + 1];
-              E[d][i][j + 1][t] = v;
-            }
-      }
-      long long o = a.eoff[pr] + (long long)k * nnz;
-      for (int xa = la; xa >= 0; --xa)
-        for (int ya = la - xa; ya >= 0; --ya) {
-          const int za = la - xa - ya;
-          const double na = comp_norm(xa) * comp_norm(ya) * comp_norm(za);
-          for (int xb = lb; xb >= 0; --xb)
-            for (int yb = lb - xb; yb >= 0; --yb) {
-              const int zb = lb - xb - yb;
-              const double c = K * na * comp_norm(xb) * comp_norm(yb) * comp_norm(zb);
-              for (int t = 0; t <= xa + xb; ++t)
-                for (int u = 0; u <= ya + yb; ++u)
-                  for (int v = 0; v <= za + zb; ++v) {
-                    const double e = c * E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][v];
-                    a.E64[o] = e;
-                    if (a.E32) a.E32[o] = float(e);
-                    ++o;
-                  }
-            }
-        }
+  const int nkeep = a.keep ? a.prc[pr] : Ka * Kb;
+  for (int k = 0; k < nkeep; ++k) {
+    const int kk = a.keep ? __ldg(a.keep + a.prb[pr] + k) : k;
+    const int ka = kk / Kb, kb = kk - ka * Kb;
+    const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+    const double p = ea + eb, ip = 1.0 / p, mu = ea * eb * ip;
+    const double Px = (ea * Ax + eb * Bx) * ip, Py = (ea * Ay + eb * By) * ip, Pz = (ea * Az + eb * Bz) * ip;
+    const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * ip;
+    const long long pp = a.prb[pr] + k;
+    a.pP[pp] = make_double4_32a(p, Px, Py, Pz);
+    if (a.pPf) {
+      const float hx = float(Px), hy = float(Py), hz = float(Pz);
+      a.pPf[2 * pp] = make_float4(float(p), hx, hy, hz);
+      a.pPf[2 * pp + 1] = make_float4(0.f, float(Px - hx), float(Py - hy), float(Pz - hz));
     }
+    // 1D tables E[d][i][j][t], i<=2, j<=2, t<=4
+    double E[3][3][3][5];
+    const double i2p = 0.5 * ip;
+    for (int d = 0; d < 3; ++d) {
+      const double XPA = -(eb * ip) * AB[d], XPB = (ea * ip) * AB[d];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          for (int t = 0; t < 5; ++t) E[d][i][j][t] = 0.0;
+      E[d][0][0][0] = 1.0;
+      for (int i = 0; i < la; ++i)
+        for (int t = 0; t <= i + 1; ++t) {
+          double v = XPA * E[d][i][0][t];
+          if (t > 0) v += i2p * E[d][i][0][t - 1];
+          if (t + 1 <= i) v += (t + 1) * E[d][i][0][t + 1];
+          E[d][i + 1][0][t] = v;
+        }
+      for (int j = 0; j < lb; ++j)
+        for (int i = 0; i <= la; ++i)
+          for (int t = 0; t <= i + j + 1; ++t) {
+            double v = XPB * E[d][i][j][t];
+            if (t > 0) v += i2p * E[d][i][j][t - 1];
+            if (t + 1 <= i + j) v += (t + 1) * E[d][i][j][t + 1];
+            E[d][i][j + 1][t] = v;
+          }
+    }
+    long long o = a.eoff[pr] + (long long)k * nnz;
+    for (int xa = la; xa >= 0; --xa)
+      for (int ya = la - xa; ya >= 0; --ya) {
+        const int za = la - xa - ya;
+        const double na = comp_norm(xa) * comp_norm(ya) * comp_norm(za);
+        for (int xb = lb; xb >= 0; --xb)
+          for (int yb = lb - xb; yb >= 0; --yb) {
+            const int zb = lb - xb - yb;
+            const double c = K * na * comp_norm(xb) * comp_norm(yb) * comp_norm(zb);
+            for (int t = 0; t <= xa + xb; ++t)
+              for (int u = 0; u <= ya + yb; ++u)
+                for (int v = 0; v <= za + zb; ++v) {
+                  const double e = c * E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][v];
+                  a.E64[o] = e;
+                  if (a.E32) a.E32[o] = float(e);
+                  ++o;
+                }
+          }
+      }
+  }
 }
 
 // sqrt of the screen table (FP64 and FP32 copies)
@@ -426,6 +430,47 @@ __global__ void k_sqrt_screen(const double* screen, double* sq, float* sqf, long
 }
 
 // ------------------------------------------------------------------ set basis
+// At most kMaxGroups primitive-count groups per pair-class list, so that a class has
+// at most kMaxGroups^2 (bra group, ket group) buckets.
+static const int kMaxGroups = 16;
+
+// Partition of the sorted distinct primitive counts vals (with their frequencies)
+// into at most gmax contiguous ranges minimising the idle lane iterations
+// sum_t freq_t (max of its range - vals_t); returns the range index of every value.
+static std::vector<int> group_counts(const std::vector<int>& vals, const std::vector<long long>& freq, int gmax) {
+  const int m = (int)vals.size();
+  std::vector<int> grp(m);
+  if (m <= gmax) {
+    for (int i = 0; i < m; ++i) grp[i] = i;
+    return grp;
+  }
+  std::vector<double> F(m + 1, 0.0), S(m + 1, 0.0);
+  for (int i = 0; i < m; ++i) {
+    F[i + 1] = F[i] + double(freq[i]);
+    S[i + 1] = S[i] + double(freq[i]) * vals[i];
+  }
+  auto cost = [&](int i, int j) { return double(vals[j]) * (F[j + 1] - F[i]) - (S[j + 1] - S[i]); };
+  const double inf = 1e300;
+  std::vector<std::vector<double>> dp(gmax + 1, std::vector<double>(m, inf));
+  std::vector<std::vector<int>> cut(gmax + 1, std::vector<int>(m, 0));
+  for (int j = 0; j < m; ++j) dp[1][j] = cost(0, j);
+  for (int g = 2; g <= gmax; ++g)
+    for (int j = g - 1; j < m; ++j)
+      for (int i = g - 1; i <= j; ++i) {
+        const double c = dp[g - 1][i - 1] + cost(i, j);
+        if (c < dp[g][j]) {
+          dp[g][j] = c;
+          cut[g][j] = i;
+        }
+      }
+  for (int g = gmax, j = m - 1; g >= 1; --g) {
+    const int i = g > 1 ? cut[g][j] : 0;
+    for (int t = i; t <= j; ++t) grp[t] = g - 1;
+    j = i - 1;
+  }
+  return grp;
+}
+
 extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, int nshell, const int* shell_mol,
                               const int* shell_L, const int* shell_nprim, const double* shell_center,
                               const double* prim_exp, const double* prim_coef, const int* shell_func) {
@@ -536,6 +581,8 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
     a.pa = h->d_pa.p;
     a.pb = h->d_pb.p;
     a.prb = h->d_prb.p;
+    a.keep = nullptr;
+    a.prc = nullptr;
     a.eoff = h->d_eoff.p;
     a.L = h->d_L.p;
     a.nprim = h->d_nprim.p;
@@ -574,6 +621,118 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
     k_sqrt_screen<<<(unsigned)((n + 255) / 256), 256>>>(h->d_screen.p, h->d_sq.p, h->d_sqf.p, n);
     CUDA_TRY(cudaGetLastError());
   }
+  // ---- primitive-pair pruning.  q_k = max over the diagonal components of
+  // sqrt((a_i b_j|a_i b_j)) of one primitive pair k = (i, j), contraction weights
+  // included (the Schwarz kernels run on "pairs" of one primitive each).  By
+  // Cauchy-Schwarz a primitive quartet is bounded by q_k q_l <= q_k q_max, so dropping
+  // the pairs with q_k q_max < prim_tol changes no contracted ERI by more than
+  // (primitive quartets of the shell quartet) x prim_tol: 1.3e-15 at 1e-18 for
+  // 36 x 36 primitive pairs, far below the 1e-12 screening of formPT.  The dropped
+  // pairs are the tight-tight products on distant centres (Gaussian factor
+  // exp(-mu |AB|^2) underflowing).  The largest pair of every shell pair is kept.
+  if (h->prim_tol > 0.0 && npp > h->npair) {
+    std::vector<int> xa(npp), xb(npp), xrb(npp), xrc(npp, 1);
+    std::vector<long long> xeo(npp);
+    std::vector<std::vector<int>> xl(kNumPairClasses);
+    for (int p = 0; p < h->npair; ++p) {
+      const int nz = nnz_pair(shell_L[h->pa[p]], shell_L[h->pb[p]]);
+      for (int k = 0; k < h->pr_count[p]; ++k) {
+        const int x = h->pr_begin[p] + k;
+        xa[x] = h->pa[p];
+        xb[x] = h->pb[p];
+        xrb[x] = x;
+        xeo[x] = h->e_off[p] + (long long)k * nz;
+        xl[h->pcls[p]].push_back(x);
+      }
+    }
+    std::vector<float> qp(npp);
+    {
+      DevBuf<int> dxa, dxb, dxrb, dxrc, dlist[kNumPairClasses];
+      DevBuf<long long> dxeo;
+      DevBuf<float> dqp;
+      DevBuf<double> dscr;
+      if (dxa.upload(xa) != cudaSuccess || dxb.upload(xb) != cudaSuccess || dxrb.upload(xrb) != cudaSuccess ||
+          dxrc.upload(xrc) != cudaSuccess || dxeo.upload(xeo) != cudaSuccess || dqp.alloc(npp) != cudaSuccess ||
+          dscr.alloc(1) != cudaSuccess)
+        return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation (primitive screening)");
+      CUDA_TRY(cudaMemset(dqp.p, 0, sizeof(float) * npp));
+      Geometry gx = h->geom();
+      gx.pa = dxa.p;
+      gx.pb = dxb.p;
+      gx.pr_begin = dxrb.p;
+      gx.pr_count = dxrc.p;
+      gx.e_off = dxeo.p;
+      SchwarzArgs sx{dscr.p, dqp.p, 1};
+      for (int c = 0; c < kNumPairClasses; ++c) {
+        if (xl[c].empty()) continue;
+        if (dlist[c].upload(xl[c]) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
+        const ClassEntry* ce = nullptr;
+        for (const ClassEntry& e : kClasses)
+          if (pair_class(e.la, e.lb) == c && pair_class(e.lc, e.ld) == c) ce = &e;
+        CUDA_TRY(ce->schwarz(gx, sx, dlist[c].p, (int)xl[c].size(), 0));
+      }
+      CUDA_TRY(cudaDeviceSynchronize());
+      CUDA_TRY(cudaMemcpy(qp.data(), dqp.p, sizeof(float) * npp, cudaMemcpyDeviceToHost));
+    }
+    float qmax = 0.f;
+    for (float v : qp) qmax = std::max(qmax, v);
+    std::vector<int> keep;
+    long long np2 = 0, ne2 = 0;
+    for (int p = 0; p < h->npair; ++p) {
+      const int nz = nnz_pair(shell_L[h->pa[p]], shell_L[h->pb[p]]);
+      const int b0 = h->pr_begin[p], n0 = h->pr_count[p];
+      int best = 0;
+      for (int k = 1; k < n0; ++k)
+        if (qp[b0 + k] > qp[b0 + best]) best = k;
+      int kept = 0;
+      for (int k = 0; k < n0; ++k)
+        if (k == best || double(qp[b0 + k]) * double(qmax) >= h->prim_tol) {
+          keep.push_back(k);
+          ++kept;
+        }
+      h->pr_begin[p] = (int)np2;
+      h->pr_count[p] = kept;
+      h->e_off[p] = ne2;
+      np2 += kept;
+      ne2 += (long long)kept * nz;
+    }
+    if (np2 < npp) {
+      h->d_pP.release();
+      h->d_pPf.release();
+      h->d_E64.release();
+      h->d_E32.release();
+      DevBuf<int> dkeep;
+      if (dkeep.upload(keep) != cudaSuccess || h->d_prb.upload(h->pr_begin) != cudaSuccess ||
+          h->d_prc.upload(h->pr_count) != cudaSuccess || h->d_eoff.upload(h->e_off) != cudaSuccess ||
+          h->d_pP.alloc(np2) != cudaSuccess || h->d_pPf.alloc(2 * np2) != cudaSuccess ||
+          h->d_E64.alloc(ne2) != cudaSuccess || h->d_E32.alloc(ne2) != cudaSuccess)
+        return fail(MMDG_E_NOMEM, "mmdg_set_basis: device allocation failed (pruned pairs)");
+      PairBuildArgs a;
+      a.npair = h->npair;
+      a.pa = h->d_pa.p;
+      a.pb = h->d_pb.p;
+      a.prb = h->d_prb.p;
+      a.keep = dkeep.p;
+      a.prc = h->d_prc.p;
+      a.eoff = h->d_eoff.p;
+      a.L = h->d_L.p;
+      a.nprim = h->d_nprim.p;
+      a.poff = h->d_poff.p;
+      a.center = h->d_center.p;
+      a.exps = h->d_exp.p;
+      a.coefs = h->d_coef.p;
+      a.pP = h->d_pP.p;
+      a.pPf = h->d_pPf.p;
+      a.E64 = h->d_E64.p;
+      a.E32 = h->d_E32.p;
+      k_build_pairs<<<(h->npair + 127) / 128, 128>>>(a);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaDeviceSynchronize());
+      npp = np2;
+      h->nprimpair = np2;
+      h->nE = ne2;
+    }
+  }
   // ---- sorted class lists: molecule, primitive count ascending, Q descending
   std::vector<float> Q(h->npair);
   CUDA_TRY(cudaMemcpy(Q.data(), h->d_Q.p, sizeof(float) * h->npair, cudaMemcpyDeviceToHost));
@@ -595,17 +754,27 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
     for (int x : v) moff[shell_mol[h->pa[x]] + 1]++;
     for (int m = 0; m < nmol; ++m) moff[m + 1] += moff[m];
     if (h->d_cls_moff[c].upload(moff) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
-    // primitive-count groups: rank of the pair's primitive count among the class's values
+    // primitive-count groups: contiguous ranges of the class's primitive counts (one
+    // per distinct count when there are at most kMaxGroups of them)
+    std::vector<int> all;
+    for (int x : v) all.push_back(h->pr_count[x]);
+    std::sort(all.begin(), all.end());
     std::vector<int> vals;
-    for (int x : v) vals.push_back(h->pr_count[x]);
-    std::sort(vals.begin(), vals.end());
-    vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
+    std::vector<long long> freq;
+    for (int x : all) {
+      if (vals.empty() || vals.back() != x) {
+        vals.push_back(x);
+        freq.push_back(0);
+      }
+      ++freq.back();
+    }
+    const std::vector<int> grp = group_counts(vals, freq, kMaxGroups);
     std::vector<int> gs(v.size()), ms(v.size());
     for (size_t i = 0; i < v.size(); ++i) {
-      gs[i] = int(std::lower_bound(vals.begin(), vals.end(), h->pr_count[v[i]]) - vals.begin());
+      gs[i] = grp[std::lower_bound(vals.begin(), vals.end(), h->pr_count[v[i]]) - vals.begin()];
       ms[i] = shell_mol[h->pa[v[i]]];
     }
-    h->ngroup[c] = (int)vals.size();
+    h->ngroup[c] = vals.empty() ? 0 : grp.back() + 1;
     if (h->d_gslot[c].upload(gs) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_set_basis: allocation");
     slot_group[c] = gs;
     slot_mol[c] = ms;
@@ -1332,6 +1501,77 @@ extern "C" int mmdg_set_tuning(mmdg_context* h, int cls, int grid_blocks) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ nuclear gradient
+#include "grad.cuh"
+
+extern "C" int mmdg_rhf_gradient(mmdg_context* h, const double* P, const double* W, int natom,
+                                 const double* atom_xyz, const double* atom_Z, const int* shell_atom, double* grad,
+                                 void* stream) {
+  if (!h || !P || !W || !atom_xyz || !atom_Z || !shell_atom || !grad || natom < 1)
+    return fail(MMDG_E_ARG, "mmdg_rhf_gradient: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_rhf_gradient: no basis set");
+  if (h->nmol != 1) return fail(MMDG_E_ARG, "mmdg_rhf_gradient: one molecule per context");
+  for (int s = 0; s < h->nshell; ++s)
+    if (shell_atom[s] < 0 || shell_atom[s] >= natom) return fail(MMDG_E_ARG, "mmdg_rhf_gradient: shell_atom out of range");
+  DeviceGuard dgd(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  DevBuf<double> dxyz, dZ, dg;
+  DevBuf<int> dsa;
+  if (dxyz.upload(std::vector<double>(atom_xyz, atom_xyz + 3 * natom)) != cudaSuccess ||
+      dZ.upload(std::vector<double>(atom_Z, atom_Z + natom)) != cudaSuccess ||
+      dsa.upload(std::vector<int>(shell_atom, shell_atom + h->nshell)) != cudaSuccess ||
+      dg.alloc(3 * (size_t)natom) != cudaSuccess)
+    return fail(MMDG_E_NOMEM, "mmdg_rhf_gradient: allocation");
+  CUDA_TRY(cudaMemsetAsync(dg.p, 0, sizeof(double) * 3 * natom, st));
+  GradArgs a;
+  a.npair = h->npair;
+  a.pa = h->d_pa.p;
+  a.pb = h->d_pb.p;
+  a.L = h->d_L.p;
+  a.nprim = h->d_nprim.p;
+  a.poff = h->d_poff.p;
+  a.func = h->d_func.p;
+  a.shell_atom = dsa.p;
+  a.center = h->d_center.p;
+  a.exps = h->d_exp.p;
+  a.coefs = h->d_coef.p;
+  a.Qpair = nullptr;
+  a.qtol = 0.0;
+  a.natom = natom;
+  a.xyz = dxyz.p;
+  a.Z = dZ.p;
+  a.P = P;
+  a.W = W;
+  a.N = h->mol_n[0];
+  a.grad = dg.p;
+  CUDA_TRY(mmdg_launch_rhf_gradient(a, st));
+  std::vector<double> g(3 * (size_t)natom);
+  CUDA_TRY(cudaMemcpyAsync(g.data(), dg.p, sizeof(double) * 3 * natom, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  // nuclear repulsion: d/dR_A sum_{B<C} Z_B Z_C / R_BC (mmd/forces.py:50-58)
+  for (int A = 0; A < natom; ++A)
+    for (int B = 0; B < natom; ++B) {
+      if (A == B) continue;
+      double d[3], r2 = 0.0;
+      for (int x = 0; x < 3; ++x) {
+        d[x] = atom_xyz[3 * A + x] - atom_xyz[3 * B + x];
+        r2 += d[x] * d[x];
+      }
+      if (r2 == 0.0) continue;
+      const double r3 = r2 * std::sqrt(r2);
+      for (int x = 0; x < 3; ++x) g[3 * A + x] -= atom_Z[A] * atom_Z[B] * d[x] / r3;
+    }
+  for (int i = 0; i < 3 * natom; ++i) grad[i] = g[i];
+  return MMDG_OK;
+}
+
+extern "C" int mmdg_set_prim_tol(mmdg_context* h, double tol) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_prim_tol: null context");
+  if (!(tol >= 0.0) || !std::isfinite(tol)) return fail(MMDG_E_ARG, "mmdg_set_prim_tol: tolerance must be >= 0");
+  h->prim_tol = tol;
   return MMDG_OK;
 }
 

@@ -1,0 +1,474 @@
+// grad.cu -- analytic RHF nuclear gradient on the GPU.
+//
+// dE/dR_A = 2 sum_ij P_ij dH_ij/dR_A - 2 sum_ij W_ij dS_ij/dR_A
+//         + sum_ijkl (2 P_ij P_kl - P_ik P_jl) d(ij|kl)/dR_A + dV_nn/dR_A
+// with W = P F P, the reference's expression (mmd/forces.py:61-97, P = C_occ C_occ^T),
+// evaluated without ever forming a derivative-integral tensor: every thread computes
+// the derivative integrals of one shell pair (one-electron terms) or one unique shell
+// quartet (two-electron terms) and contracts them at once with the densities.
+//
+// Derivatives of a Cartesian Gaussian with respect to its centre (cython/grad.pyx:
+// 101-108): d/dA_x G_i = 2a G_{i+1} - i G_{i-1}, so the Hermite coefficients of a
+// differentiated product are 2a E^{i+1,j}_t - i E^{i-1,j}_t (centre A) or
+// 2b E^{i,j+1}_t - j E^{i,j-1}_t (centre B).  Translational invariance gives the
+// remaining centre: d/dD = -(d/dA + d/dB + d/dC) for a quartet, d/dB = -d/dA for the
+// overlap and kinetic integrals, and d/dC = -(d/dA + d/dB) for the attraction of
+// nucleus C (its Hellmann-Feynman term).
+//
+// These kernels are generic (runtime loops over angular momenta, s..d shells, total
+// angular momentum up to 9), one launch per gradient; the Boys function comes from its
+// defining series (downward recursion) below T = 35 and from upward recursion off
+// F_0 = sqrt(pi/T)/2 erf(sqrt T) above.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "grad.cuh"
+
+namespace {
+
+constexpr int kLmaxShell = 2;                 // d shells
+constexpr int kEi = kLmaxShell + 2;           // i (or j) up to l + 1 (ERI) / l + 2 (kinetic)
+constexpr int kEj = kLmaxShell + 3;
+constexpr int kEt = 2 * kLmaxShell + 4;       // t up to i + j
+constexpr int kLtot = 4 * kLmaxShell + 1;     // total angular momentum of a differentiated quartet
+constexpr int kRsize = (kLtot + 1) * (kLtot + 2) * (kLtot + 3) / 6;
+constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ double comp_norm(int l) { return l >= 2 ? 0.57735026918962576 : 1.0; }
+
+// Cartesian exponents of component c of a shell of angular momentum L (the order of
+// mmd/molecule.py:104-115: x^L first, then decreasing x, then decreasing y)
+__device__ __forceinline__ void lmn_of(int L, int c, int& l, int& m, int& n) {
+  int k = 0;
+  for (int x = L; x >= 0; --x)
+    for (int y = L - x; y >= 0; --y) {
+      if (k == c) {
+        l = x;
+        m = y;
+        n = L - x - y;
+        return;
+      }
+      ++k;
+    }
+  l = m = n = 0;
+}
+
+// 1D Hermite expansion coefficients E[i][j][t] of G_i(x; a, A) G_j(x; b, B) for
+// i <= imax, j <= jmax (cython/util.pxi:13-28 recursion; the Gaussian factor is
+// applied by the caller)
+struct E1 {
+  double v[kEi][kEj][kEt];
+};
+
+__device__ void hermite_1d(E1& E, int imax, int jmax, double p, double XPA, double XPB) {
+  const double i2p = 0.5 / p;
+  for (int i = 0; i <= imax; ++i)
+    for (int j = 0; j <= jmax; ++j)
+      for (int t = 0; t < kEt; ++t) E.v[i][j][t] = 0.0;
+  E.v[0][0][0] = 1.0;
+  for (int i = 0; i < imax; ++i)
+    for (int t = 0; t <= i + 1; ++t) {
+      double v = XPA * E.v[i][0][t];
+      if (t > 0) v += i2p * E.v[i][0][t - 1];
+      if (t + 1 <= i) v += (t + 1) * E.v[i][0][t + 1];
+      E.v[i + 1][0][t] = v;
+    }
+  for (int j = 0; j < jmax; ++j)
+    for (int i = 0; i <= imax; ++i)
+      for (int t = 0; t <= i + j + 1 && t < kEt; ++t) {
+        double v = XPB * E.v[i][j][t];
+        if (t > 0) v += i2p * E.v[i][j][t - 1];
+        if (t + 1 <= i + j) v += (t + 1) * E.v[i][j][t + 1];
+        E.v[i][j + 1][t] = v;
+      }
+}
+
+// F_m(T), m = 0..M (M <= kLtot + 1)
+__device__ void boys_series(int M, double T, double* F) {
+  const double e = exp(-T);
+  if (T < 35.0) {
+    double term = 1.0 / (2 * M + 1), sum = term;
+    for (int i = 0; i < 400; ++i) {
+      term *= 2.0 * T / (2 * M + 2 * i + 3);
+      sum += term;
+      if (term < 1e-17 * sum) break;
+    }
+    F[M] = e * sum;
+    for (int m = M; m > 0; --m) F[m - 1] = (2.0 * T * F[m] + e) / (2 * m - 1);
+  } else {
+    const double st = sqrt(T);
+    F[0] = 0.5 * sqrt(kPi) / st * erf(st);
+    for (int m = 0; m < M; ++m) F[m + 1] = ((2 * m + 1) * F[m] - e) / (2.0 * T);
+  }
+}
+
+// packed Hermite index of (t, u, v): order k = t+u+v, then s = u+v, then v
+__device__ __forceinline__ int ridx(int t, int u, int v) {
+  const int k = t + u + v, s = u + v;
+  return k * (k + 1) * (k + 2) / 6 + s * (s + 1) / 2 + v;
+}
+
+// R_{tuv}(alpha, X, Y, Z) for t+u+v <= M in place (cython/util.pxi:33-50 recursion,
+// run downward in the auxiliary index n over a single buffer)
+__device__ void hermite_r(int M, double alpha, double X, double Y, double Z, const double* F, double* R) {
+  double f = 1.0;
+  for (int n = M; n >= 0; --n) {
+    // orders M-n .. 1 of level n from level n+1 (descending order keeps inputs intact)
+    for (int k = M - n; k >= 1; --k)
+      for (int t = k; t >= 0; --t)
+        for (int u = k - t; u >= 0; --u) {
+          const int v = k - t - u;
+          double r;
+          if (t > 0) {
+            r = X * R[ridx(t - 1, u, v)];
+            if (t > 1) r += (t - 1) * R[ridx(t - 2, u, v)];
+          } else if (u > 0) {
+            r = Y * R[ridx(t, u - 1, v)];
+            if (u > 1) r += (u - 1) * R[ridx(t, u - 2, v)];
+          } else {
+            r = Z * R[ridx(t, u, v - 1)];
+            if (v > 1) r += (v - 1) * R[ridx(t, u, v - 2)];
+          }
+          R[ridx(t, u, v)] = r;
+        }
+    f = 1.0;
+    for (int i = 0; i < n; ++i) f *= -2.0 * alpha;
+    R[0] = f * F[n];
+  }
+}
+
+// ------------------------------------------------------------------ one-electron terms
+__global__ void k_grad_one(GradArgs a) {
+  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= a.npair) return;
+  const int sa = a.pa[pr], sb = a.pb[pr];
+  const int la = a.L[sa], lb = a.L[sb];
+  const int Ka = a.nprim[sa], Kb = a.nprim[sb];
+  const int atA = a.shell_atom[sa], atB = a.shell_atom[sb];
+  const double A[3] = {a.center[3 * sa], a.center[3 * sa + 1], a.center[3 * sa + 2]};
+  const double B[3] = {a.center[3 * sb], a.center[3 * sb + 1], a.center[3 * sb + 2]};
+  const double fac = sa == sb ? 1.0 : 2.0;  // (i, j) and (j, i) of two different shells
+  const int nca = (la + 1) * (la + 2) / 2, ncb = (lb + 1) * (lb + 2) / 2;
+  double gA[3] = {0, 0, 0};
+  E1 E[3];
+  double R[kRsize], F[kLtot + 2];
+  // ---- overlap and kinetic: d/dB = -d/dA
+  for (int ka = 0; ka < Ka; ++ka)
+    for (int kb = 0; kb < Kb; ++kb) {
+      const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+      const double p = ea + eb, mu = ea * eb / p;
+      double AB2 = 0.0;
+      for (int d = 0; d < 3; ++d) AB2 += (A[d] - B[d]) * (A[d] - B[d]);
+      const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb];
+      const double sq = sqrt(kPi / p);
+      for (int d = 0; d < 3; ++d)
+        hermite_1d(E[d], la + 1, lb + 2, p, -(eb / p) * (A[d] - B[d]), (ea / p) * (A[d] - B[d]));
+      for (int ca = 0; ca < nca; ++ca) {
+        const int fi = a.func[sa * kGradMaxComp + ca];
+        if (fi < 0) continue;
+        int ia[3];
+        lmn_of(la, ca, ia[0], ia[1], ia[2]);
+        for (int cb = 0; cb < ncb; ++cb) {
+          const int fj = a.func[sb * kGradMaxComp + cb];
+          if (fj < 0) continue;
+          int jb[3];
+          lmn_of(lb, cb, jb[0], jb[1], jb[2]);
+          const double nrm = comp_norm(ia[0]) * comp_norm(ia[1]) * comp_norm(ia[2]) * comp_norm(jb[0]) *
+                             comp_norm(jb[1]) * comp_norm(jb[2]);
+          const double Pij = a.P[(long long)fi * a.N + fj], Wij = a.W[(long long)fi * a.N + fj];
+          // 1D overlap S(i, j) and kinetic T(i, j) (cython/onee.pyx:103-133 decomposition)
+          auto S1 = [&](int d, int i, int j) { return (i < 0 || j < 0) ? 0.0 : E[d].v[i][j][0] * sq; };
+          auto T1 = [&](int d, int i, int j) {
+            if (i < 0) return 0.0;
+            double t = eb * (2 * j + 1) * S1(d, i, j) - 2.0 * eb * eb * S1(d, i, j + 2);
+            if (j >= 2) t -= 0.5 * j * (j - 1) * S1(d, i, j - 2);
+            return t;
+          };
+          for (int d = 0; d < 3; ++d) {
+            // derivative in direction d of the bra: 2a f(i+1) - i f(i-1)
+            double dS = 1.0, dT = 0.0;
+            double Sd[3], Td[3];
+            for (int e = 0; e < 3; ++e) {
+              if (e == d) {
+                Sd[e] = 2.0 * ea * S1(e, ia[e] + 1, jb[e]) - ia[e] * S1(e, ia[e] - 1, jb[e]);
+                Td[e] = 2.0 * ea * T1(e, ia[e] + 1, jb[e]) - ia[e] * T1(e, ia[e] - 1, jb[e]);
+              } else {
+                Sd[e] = S1(e, ia[e], jb[e]);
+                Td[e] = T1(e, ia[e], jb[e]);
+              }
+            }
+            dS = Sd[0] * Sd[1] * Sd[2];
+            dT = Td[0] * Sd[1] * Sd[2] + Sd[0] * Td[1] * Sd[2] + Sd[0] * Sd[1] * Td[2];
+            gA[d] += fac * K * nrm * (2.0 * Pij * dT - 2.0 * Wij * dS);
+          }
+        }
+      }
+    }
+  for (int d = 0; d < 3; ++d) {
+    atomicAdd(a.grad + 3 * atA + d, gA[d]);
+    atomicAdd(a.grad + 3 * atB + d, -gA[d]);
+  }
+  // ---- nuclear attraction, one nucleus at a time: basis terms on A and B, and the
+  // Hellmann-Feynman term on the nucleus, -(A + B)
+  for (int c = 0; c < a.natom; ++c) {
+    const double C[3] = {a.xyz[3 * c], a.xyz[3 * c + 1], a.xyz[3 * c + 2]};
+    const double Zc = a.Z[c];
+    double vA[3] = {0, 0, 0}, vB[3] = {0, 0, 0};
+    for (int ka = 0; ka < Ka; ++ka)
+      for (int kb = 0; kb < Kb; ++kb) {
+        const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+        const double p = ea + eb, mu = ea * eb / p;
+        double AB2 = 0.0, P[3];
+        for (int d = 0; d < 3; ++d) {
+          AB2 += (A[d] - B[d]) * (A[d] - B[d]);
+          P[d] = (ea * A[d] + eb * B[d]) / p;
+        }
+        const double K = exp(-mu * AB2) * a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb];
+        for (int d = 0; d < 3; ++d)
+          hermite_1d(E[d], la + 1, lb + 1, p, -(eb / p) * (A[d] - B[d]), (ea / p) * (A[d] - B[d]));
+        const int M = la + lb + 1;
+        const double X = P[0] - C[0], Y = P[1] - C[1], Z = P[2] - C[2];
+        boys_series(M, p * (X * X + Y * Y + Z * Z), F);
+        hermite_r(M, p, X, Y, Z, F, R);
+        const double pref = -Zc * 2.0 * kPi / p * K;
+        for (int ca = 0; ca < nca; ++ca) {
+          const int fi = a.func[sa * kGradMaxComp + ca];
+          if (fi < 0) continue;
+          int ia[3];
+          lmn_of(la, ca, ia[0], ia[1], ia[2]);
+          for (int cb = 0; cb < ncb; ++cb) {
+            const int fj = a.func[sb * kGradMaxComp + cb];
+            if (fj < 0) continue;
+            int jb[3];
+            lmn_of(lb, cb, jb[0], jb[1], jb[2]);
+            const double nrm = comp_norm(ia[0]) * comp_norm(ia[1]) * comp_norm(ia[2]) * comp_norm(jb[0]) *
+                               comp_norm(jb[1]) * comp_norm(jb[2]);
+            const double w = fac * 2.0 * a.P[(long long)fi * a.N + fj] * pref * nrm;
+            // V(i, j) with one index of one dimension shifted by s = +-1 on centre A or B
+            auto V = [&](int d, int ia_d, int jb_d) {
+              if (ia_d < 0 || jb_d < 0) return 0.0;
+              int ii[3] = {ia[0], ia[1], ia[2]}, jj[3] = {jb[0], jb[1], jb[2]};
+              ii[d] = ia_d;
+              jj[d] = jb_d;
+              double s = 0.0;
+              for (int t = 0; t <= ii[0] + jj[0]; ++t)
+                for (int u = 0; u <= ii[1] + jj[1]; ++u)
+                  for (int v = 0; v <= ii[2] + jj[2]; ++v)
+                    s += E[0].v[ii[0]][jj[0]][t] * E[1].v[ii[1]][jj[1]][u] * E[2].v[ii[2]][jj[2]][v] *
+                         R[ridx(t, u, v)];
+              return s;
+            };
+            for (int d = 0; d < 3; ++d) {
+              vA[d] += w * (2.0 * ea * V(d, ia[d] + 1, jb[d]) - ia[d] * V(d, ia[d] - 1, jb[d]));
+              vB[d] += w * (2.0 * eb * V(d, ia[d], jb[d] + 1) - jb[d] * V(d, ia[d], jb[d] - 1));
+            }
+          }
+        }
+      }
+    for (int d = 0; d < 3; ++d) {
+      atomicAdd(a.grad + 3 * atA + d, vA[d]);
+      atomicAdd(a.grad + 3 * atB + d, vB[d]);
+      atomicAdd(a.grad + 3 * c + d, -(vA[d] + vB[d]));
+    }
+  }
+}
+
+// ------------------------------------------------------------------ two-electron terms
+// One thread per unique shell quartet (bra pair ip >= ket pair iq); every unique
+// function quartet once, with the degeneracy of cython/fock.pyx:60-70 and the density
+// factor 2 P_ij P_kl - (P_ik P_jl + P_il P_jk) / 2 (the exchange term averaged over the
+// quartet's permutations).
+__global__ void k_grad_two(GradArgs a) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nq = (long long)a.npair * (a.npair + 1) / 2;
+  if (q >= nq) return;
+  // (ip, iq) from the triangular index q = ip (ip + 1) / 2 + iq
+  int ip = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+  while ((long long)ip * (ip + 1) / 2 > q) --ip;
+  while ((long long)(ip + 1) * (ip + 2) / 2 <= q) ++ip;
+  const int iq = (int)(q - (long long)ip * (ip + 1) / 2);
+  if (a.Qpair && (double)a.Qpair[ip] * (double)a.Qpair[iq] < a.qtol) return;
+  const int s[4] = {a.pa[ip], a.pb[ip], a.pa[iq], a.pb[iq]};
+  int Ls[4], nc[4];
+  for (int k = 0; k < 4; ++k) {
+    Ls[k] = a.L[s[k]];
+    nc[k] = (Ls[k] + 1) * (Ls[k] + 2) / 2;
+  }
+  const bool same_ab = s[0] == s[1], same_cd = s[2] == s[3], same_pair = ip == iq;
+  double Cn[4][3];
+  for (int k = 0; k < 4; ++k)
+    for (int d = 0; d < 3; ++d) Cn[k][d] = a.center[3 * s[k] + d];
+  double g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // centres a, b, c
+  E1 Eb[3], Ek[3];
+  double R[kRsize], F[kLtot + 2];
+  double W[6 * 6 * 6];
+  const int N = a.N;
+  for (int k0 = 0; k0 < a.nprim[s[0]]; ++k0)
+    for (int k1 = 0; k1 < a.nprim[s[1]]; ++k1) {
+      const double ea = a.exps[a.poff[s[0]] + k0], eb = a.exps[a.poff[s[1]] + k1];
+      const double p = ea + eb;
+      double AB2 = 0.0, P[3];
+      for (int d = 0; d < 3; ++d) {
+        AB2 += (Cn[0][d] - Cn[1][d]) * (Cn[0][d] - Cn[1][d]);
+        P[d] = (ea * Cn[0][d] + eb * Cn[1][d]) / p;
+      }
+      const double Kab = exp(-ea * eb / p * AB2) * a.coefs[a.poff[s[0]] + k0] * a.coefs[a.poff[s[1]] + k1];
+      for (int d = 0; d < 3; ++d)
+        hermite_1d(Eb[d], Ls[0] + 1, Ls[1] + 1, p, -(eb / p) * (Cn[0][d] - Cn[1][d]), (ea / p) * (Cn[0][d] - Cn[1][d]));
+      for (int k2 = 0; k2 < a.nprim[s[2]]; ++k2)
+        for (int k3 = 0; k3 < a.nprim[s[3]]; ++k3) {
+          const double ec = a.exps[a.poff[s[2]] + k2], ed = a.exps[a.poff[s[3]] + k3];
+          const double qq = ec + ed;
+          double CD2 = 0.0, Q[3];
+          for (int d = 0; d < 3; ++d) {
+            CD2 += (Cn[2][d] - Cn[3][d]) * (Cn[2][d] - Cn[3][d]);
+            Q[d] = (ec * Cn[2][d] + ed * Cn[3][d]) / qq;
+          }
+          const double Kcd = exp(-ec * ed / qq * CD2) * a.coefs[a.poff[s[2]] + k2] * a.coefs[a.poff[s[3]] + k3];
+          for (int d = 0; d < 3; ++d)
+            hermite_1d(Ek[d], Ls[2] + 1, Ls[3] + 1, qq, -(ed / qq) * (Cn[2][d] - Cn[3][d]),
+                       (ec / qq) * (Cn[2][d] - Cn[3][d]));
+          const double alpha = p * qq / (p + qq);
+          const double X = P[0] - Q[0], Y = P[1] - Q[1], Z = P[2] - Q[2];
+          const int M = Ls[0] + Ls[1] + Ls[2] + Ls[3] + 1;
+          boys_series(M, alpha * (X * X + Y * Y + Z * Z), F);
+          hermite_r(M, alpha, X, Y, Z, F, R);
+          const double pref = 2.0 * pow(kPi, 2.5) / (p * qq * sqrt(p + qq)) * Kab * Kcd;
+          for (int ca = 0; ca < nc[0]; ++ca)
+            for (int cb = 0; cb < nc[1]; ++cb) {
+              if (same_ab && ca < cb) continue;
+              const int fi0 = a.func[s[0] * kGradMaxComp + ca], fj0 = a.func[s[1] * kGradMaxComp + cb];
+              if (fi0 < 0 || fj0 < 0) continue;
+              int la3[3], lb3[3];
+              lmn_of(Ls[0], ca, la3[0], la3[1], la3[2]);
+              lmn_of(Ls[1], cb, lb3[0], lb3[1], lb3[2]);
+              for (int cc = 0; cc < nc[2]; ++cc)
+                for (int cd = 0; cd < nc[3]; ++cd) {
+                  if (same_cd && cc < cd) continue;
+                  if (same_pair && (ca * nc[1] + cb) < (cc * nc[3] + cd)) continue;
+                  int i = fi0, j = fj0;
+                  int k = a.func[s[2] * kGradMaxComp + cc], l = a.func[s[3] * kGradMaxComp + cd];
+                  if (k < 0 || l < 0) continue;
+                  // canonical labels and degeneracy (cython/fock.pyx:24-70)
+                  if (i < j) { int t = i; i = j; j = t; }
+                  if (k < l) { int t = k; k = l; l = t; }
+                  const int ij = i * (i + 1) / 2 + j, kl = k * (k + 1) / 2 + l;
+                  if (ij < kl) {
+                    int t = i; i = k; k = t;
+                    t = j; j = l; l = t;
+                  }
+                  const double deg = (i != j ? 2.0 : 1.0) * (k != l ? 2.0 : 1.0) * (ij != kl ? 2.0 : 1.0);
+                  const double* Pm = a.P;
+                  const double gam = 2.0 * Pm[(long long)i * N + j] * Pm[(long long)k * N + l] -
+                                     0.5 * (Pm[(long long)i * N + k] * Pm[(long long)j * N + l] +
+                                            Pm[(long long)i * N + l] * Pm[(long long)j * N + k]);
+                  int lc3[3], ld3[3];
+                  lmn_of(Ls[2], cc, lc3[0], lc3[1], lc3[2]);
+                  lmn_of(Ls[3], cd, ld3[0], ld3[1], ld3[2]);
+                  const double nrm = comp_norm(la3[0]) * comp_norm(la3[1]) * comp_norm(la3[2]) *
+                                     comp_norm(lb3[0]) * comp_norm(lb3[1]) * comp_norm(lb3[2]) *
+                                     comp_norm(lc3[0]) * comp_norm(lc3[1]) * comp_norm(lc3[2]) *
+                                     comp_norm(ld3[0]) * comp_norm(ld3[1]) * comp_norm(ld3[2]);
+                  const double wgt = deg * gam * pref * nrm;
+                  if (wgt == 0.0) continue;
+                  // bra extents with one extra Hermite order for the bra derivatives
+                  const int bt = la3[0] + lb3[0] + 1, bu = la3[1] + lb3[1] + 1, bv = la3[2] + lb3[2] + 1;
+                  const int kt = lc3[0] + ld3[0], ku = lc3[1] + ld3[1], kv = lc3[2] + ld3[2];
+                  // ket-transformed R: W[t][u][v] = sum E^cd (-1)^(tau+nu+phi) R[t+tau][u+nu][v+phi]
+                  for (int t = 0; t <= bt; ++t)
+                    for (int u = 0; u <= bu; ++u)
+                      for (int v = 0; v <= bv; ++v) {
+                        double w = 0.0;
+                        for (int ta = 0; ta <= kt; ++ta)
+                          for (int nu = 0; nu <= ku; ++nu)
+                            for (int ph = 0; ph <= kv; ++ph) {
+                              const double e = Ek[0].v[lc3[0]][ld3[0]][ta] * Ek[1].v[lc3[1]][ld3[1]][nu] *
+                                               Ek[2].v[lc3[2]][ld3[2]][ph];
+                              w += ((ta + nu + ph) & 1 ? -e : e) * R[ridx(t + ta, u + nu, v + ph)];
+                            }
+                        W[(t * 6 + u) * 6 + v] = w;
+                      }
+                  // centres a and b
+                  for (int d = 0; d < 3; ++d) {
+                    double sa_ = 0.0, sb_ = 0.0;
+                    for (int t = 0; t <= bt; ++t)
+                      for (int u = 0; u <= bu; ++u)
+                        for (int v = 0; v <= bv; ++v) {
+                          const int tt[3] = {t, u, v};
+                          double ea_ = 1.0, eb_ = 1.0;
+                          for (int e = 0; e < 3; ++e) {
+                            const double base = Eb[e].v[la3[e]][lb3[e]][tt[e]];
+                            if (e == d) {
+                              double da = 2.0 * ea * Eb[e].v[la3[e] + 1][lb3[e]][tt[e]];
+                              if (la3[e] > 0) da -= la3[e] * Eb[e].v[la3[e] - 1][lb3[e]][tt[e]];
+                              double db = 2.0 * eb * Eb[e].v[la3[e]][lb3[e] + 1][tt[e]];
+                              if (lb3[e] > 0) db -= lb3[e] * Eb[e].v[la3[e]][lb3[e] - 1][tt[e]];
+                              ea_ *= da;
+                              eb_ *= db;
+                            } else {
+                              ea_ *= base;
+                              eb_ *= base;
+                            }
+                          }
+                          const double w = W[(t * 6 + u) * 6 + v];
+                          sa_ += ea_ * w;
+                          sb_ += eb_ * w;
+                        }
+                    g[0][d] += wgt * sa_;
+                    g[1][d] += wgt * sb_;
+                  }
+                  // centre c: ket derivative coefficients, bra without the extra order
+                  for (int d = 0; d < 3; ++d) {
+                    double sc_ = 0.0;
+                    const int kte[3] = {kt + (d == 0), ku + (d == 1), kv + (d == 2)};
+                    for (int t = 0; t <= bt - 1; ++t)
+                      for (int u = 0; u <= bu - 1; ++u)
+                        for (int v = 0; v <= bv - 1; ++v) {
+                          const double eab = Eb[0].v[la3[0]][lb3[0]][t] * Eb[1].v[la3[1]][lb3[1]][u] *
+                                             Eb[2].v[la3[2]][lb3[2]][v];
+                          if (eab == 0.0) continue;
+                          double w = 0.0;
+                          for (int ta = 0; ta <= kte[0]; ++ta)
+                            for (int nu = 0; nu <= kte[1]; ++nu)
+                              for (int ph = 0; ph <= kte[2]; ++ph) {
+                                const int tk[3] = {ta, nu, ph};
+                                double e = 1.0;
+                                for (int x = 0; x < 3; ++x) {
+                                  if (x == d) {
+                                    double dc = 2.0 * ec * Ek[x].v[lc3[x] + 1][ld3[x]][tk[x]];
+                                    if (lc3[x] > 0) dc -= lc3[x] * Ek[x].v[lc3[x] - 1][ld3[x]][tk[x]];
+                                    e *= dc;
+                                  } else {
+                                    e *= Ek[x].v[lc3[x]][ld3[x]][tk[x]];
+                                  }
+                                }
+                                w += ((ta + nu + ph) & 1 ? -e : e) * R[ridx(t + ta, u + nu, v + ph)];
+                              }
+                          sc_ += eab * w;
+                        }
+                    g[2][d] += wgt * sc_;
+                  }
+                }
+            }
+        }
+    }
+  const int at[4] = {a.shell_atom[s[0]], a.shell_atom[s[1]], a.shell_atom[s[2]], a.shell_atom[s[3]]};
+  for (int d = 0; d < 3; ++d) {
+    atomicAdd(a.grad + 3 * at[0] + d, g[0][d]);
+    atomicAdd(a.grad + 3 * at[1] + d, g[1][d]);
+    atomicAdd(a.grad + 3 * at[2] + d, g[2][d]);
+    atomicAdd(a.grad + 3 * at[3] + d, -(g[0][d] + g[1][d] + g[2][d]));
+  }
+}
+
+}  // namespace
+
+cudaError_t mmdg_launch_rhf_gradient(const GradArgs& a, cudaStream_t st) {
+  if (a.npair <= 0) return cudaSuccess;
+  k_grad_one<<<(a.npair + 63) / 64, 64, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long long nq = (long long)a.npair * (a.npair + 1) / 2;
+  k_grad_two<<<(unsigned)((nq + 63) / 64), 64, 0, st>>>(a);
+  return cudaGetLastError();
+}

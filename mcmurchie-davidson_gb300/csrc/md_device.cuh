@@ -384,6 +384,8 @@ struct TensorDigest {
 struct SchwarzArgs {
   double* screen;  // packed per-molecule N(N+1)/2: (ij|ij)
   float* Qpair;    // per shell pair: max sqrt((ij|ij)), written via atomicMax on the bits
+  int prim;        // primitive mode: every "pair" is one primitive pair; only Qpair is
+                   // written, over all diagonal component pairs, from an FP64 square root
 };
 
 template <int NB, int ND>
@@ -400,12 +402,17 @@ struct SchwarzDigest {
   template <typename Real>
   __device__ __forceinline__ void put(int ca, int cb, int cc, int cd, Real vr) {
     if (ca != cc || cb != cd) return;
-    if (q.same_ab && ca < cb) return;
+    if (!s.prim && q.same_ab && ca < cb) return;
     int i = __ldg(g.func + q.sa * kMaxComp + ca);
     int j = __ldg(g.func + q.sb * kMaxComp + cb);
     if ((i | j) < 0) return;
     if (i < j) { int t = i; i = j; j = t; }
     const double v = double(vr);
+    if (s.prim) {
+      const float r = float(sqrt(fmax(v, 0.0)));
+      atomicMax(reinterpret_cast<int*>(s.Qpair + pair), __float_as_int(r));
+      return;
+    }
     s.screen[tbase + tri(i) + j] = v;
     const float r = sqrtf(fmaxf(float(v), 0.0f));
     atomicMax(reinterpret_cast<int*>(s.Qpair + pair), __float_as_int(r));

@@ -248,6 +248,8 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
   pa_args.pa = dpa;
   pa_args.pb = dpb;
   pa_args.prb = dprb;
+  pa_args.keep = nullptr;
+  pa_args.prc = nullptr;
   pa_args.eoff = dEoff;
   pa_args.L = dL;
   pa_args.nprim = dK;

@@ -5,6 +5,9 @@
 struct PairBuildArgs {
   int npair;
   const int *pa, *pb, *prb;
+  // optional primitive subset: pair pr builds the primitive pairs
+  // keep[prb[pr] .. prb[pr] + prc[pr]) (index ka * Kb + kb); null: all Ka * Kb
+  const int *keep, *prc;
   const long long* eoff;
   const int *L, *nprim, *poff;
   const double *center, *exps, *coefs;

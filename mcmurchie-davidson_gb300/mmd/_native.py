@@ -45,6 +45,8 @@ def _bind(L):
         "mmdg_one_electron": (c_int, [p, c_int, p, p, p, p, p, p, p, p, p]),
         "mmdg_set_tuning": (c_int, [p, c_int, c_int]),
         "mmdg_set_streams": (c_int, [p, c_int]),
+        "mmdg_set_prim_tol": (c_int, [p, ctypes.c_double]),
+        "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, p, p]),
         "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),
     }
     for name, (res, args) in sig.items():
@@ -95,7 +97,7 @@ class Context:
     ``shells`` is a ``ShellSet`` (``mmd.integrals.shells``) or a list of them (a
     batch of molecules)."""
 
-    def __init__(self, shells, device: int | None = None):
+    def __init__(self, shells, device: int | None = None, prim_tol: float | None = None):
         torch = _torch()
         self.torch = torch
         self.device = torch.cuda.current_device() if device is None else int(device)
@@ -115,6 +117,8 @@ class Context:
         fn = np.ascontiguousarray(np.concatenate([s.func for s in sets]), dtype=np.int32)
         self.nshell = len(L)
         self._keep = (mol, L, K, cen, ex, co, fn)
+        if prim_tol is not None:  # primitive-pair screening (default 1e-18; 0 keeps every pair)
+            check(lib().mmdg_set_prim_tol(h, float(prim_tol)), "mmdg_set_prim_tol")
         with torch.cuda.device(self.device):
             check(lib().mmdg_set_basis(h, self.nmol, _ptr(self.nfunc), self.nshell, _ptr(mol), _ptr(L), _ptr(K),
                                        _ptr(cen), _ptr(ex), _ptr(co), _ptr(fn)), "mmdg_set_basis")

@@ -16,6 +16,7 @@ import numpy as np
 
 from .integrals.shells import shells_from_bfs
 from .integrals.twoe import Basis, context_for
+from .forces import Forces
 from .scf import SCF
 
 ANGSTROM = 0.52917721092  # mmd/molecule.py:224-226
@@ -93,8 +94,13 @@ def get_basis(filename):
     return basis
 
 
-class Molecule(SCF):
+class Molecule(SCF, Forces):
     """Molecule with GPU integrals (mmd/molecule.py:24-315)."""
+
+    @property
+    def _forces(self):
+        """Forces of every atom, natom x 3 (mmd/molecule.py:47-53)."""
+        return np.concatenate([atom.forces for atom in self.atoms]).reshape(-1, 3)
 
     def __init__(self, geometry, basis="sto-3g"):
         charge, multiplicity, atomlist = self.read_molecule(geometry)

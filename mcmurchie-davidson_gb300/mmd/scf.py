@@ -29,7 +29,17 @@ import time
 import numpy as np
 
 # dense symmetric eigensolver of the SCF: host LAPACK up to this size, cuSOLVER above
-HOST_EIGH_MAX_N = 640
+HOST_EIGH_MAX_N = 1024
+
+
+def host_eigh(A):
+    """One symmetric eigensolve on the host cores: LAPACK dsyevd through SciPy (on the
+    Grace host 0.64 ms at N = 104 against 2.8 ms for numpy.linalg.eigh; 7.4 ms at
+    N = 400 and 28 ms at N = 800, where cuSOLVER's syevd takes 11.8 and 31 ms).  Many
+    small solves at once (the batched SCF) stay on numpy.linalg.eigh in a thread pool:
+    SciPy's wrapper serialises there (1.14 s against 0.45 s for 1024 matrices)."""
+    import scipy.linalg
+    return scipy.linalg.eigh(A, driver="evd", check_finite=False)
 # an initial guess is abandoned (restart from the core guess) when the DIIS error
 # has grown this many iterations in a row
 GUESS_FALLBACK_GROWTH = 3
@@ -183,15 +193,24 @@ class SCF(object):
             self.G = G
             self.F = self.F_old + G
         else:
+            # J and K are linear in P: a complex density (real-time TDHF) is two real
+            # builds; the results are complex like the reference's einsums
             ctx = self.context
             torch = ctx.torch
-            Pd = torch.as_tensor(np.ascontiguousarray(np.real(self.P), dtype=np.float64), device=self._dev["S"].device)
-            Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
-            ctx.jk_dense(self._dev["TwoE"], Pd, Jd, Kd)
-            self.J = Jd.cpu().numpy()
-            self.K = Kd.cpu().numpy()
+            P = np.asarray(self.P)
+            J = np.zeros(P.shape, dtype=complex)
+            K = np.zeros(P.shape, dtype=complex)
+            for scale, part in ((1.0, np.real(P)), (1j, np.imag(P))):
+                if scale != 1.0 and not np.any(part):
+                    continue
+                Pd = torch.as_tensor(np.ascontiguousarray(part, dtype=np.float64), device=self._dev["S"].device)
+                Jd, Kd = torch.empty_like(Pd), torch.empty_like(Pd)
+                ctx.jk_dense(self._dev["TwoE"], Pd, Jd, Kd)
+                J += scale * Jd.cpu().numpy()
+                K += scale * Kd.cpu().numpy()
+            self.J, self.K = J, K
             self.G = 2.0 * self.J - self.K
-            self.F = self.Core + self.G
+            self.F = self.Core.astype(complex) + self.G
 
     def updateFock(self):
         self.unOrthoDen()
@@ -264,9 +283,8 @@ class _RHFState:
         if not self.DIIS or self.step == 0:
             self.FO = X.T @ self.F @ X
         if self.FO.shape[0] <= HOST_EIGH_MAX_N:
-            # below ~640 functions LAPACK on the host cores beats cuSOLVER's syevd on
-            # GB300 (measured 7.7 vs 11.8 ms at N = 400; 26.6 vs 31.4 ms at N = 800)
-            w, v = np.linalg.eigh(self.FO.cpu().numpy())
+            # up to ~1000 functions LAPACK on the host cores beats cuSOLVER's syevd
+            w, v = host_eigh(self.FO.cpu().numpy())
             E = torch.from_numpy(w).to(self.FO.device)
             CO = torch.from_numpy(v).to(self.FO.device)
         else:

@@ -146,12 +146,14 @@ def test_formPT_vs_oracle_random_density():
 def test_rhf_energy_conventional(name):
     """Tightly converged (conver 1e-12, dE < 1e-10) energies agree to 1e-10 Eh.  At the
     default conver = 1e-8 the stopping iterate is path dependent (rounding in eigh and
-    DIIS moves it by ~1e-9), so that energy is held to the convergence scale, 1e-8."""
+    DIIS moves it), and the reference's energy pairs the last density with the Fock
+    matrix of the one before, an error first order in ||P - P_old|| < 1e-8: that
+    energy is held to 5e-8 (1.3e-8 seen on methane with a different LAPACK driver)."""
     d = _load(f"mol_{name}.npz")
     E12 = _mol(d).RHF(doPrint=False, conver=1e-12)
     assert abs(E12 - float(d["energy_conv_1e12"])) < 1e-10, (E12, float(d["energy_conv_1e12"]))
     E = _mol(d).RHF(doPrint=False)
-    assert abs(E - float(d["energy_conv"])) < 1e-8, (E, float(d["energy_conv"]))
+    assert abs(E - float(d["energy_conv"])) < 5e-8, (E, float(d["energy_conv"]))
 
 
 @pytest.mark.parametrize("name", [m for m in MOLS if "energy_direct" in _load(f"mol_{m}.npz")])
@@ -159,7 +161,7 @@ def test_rhf_energy_direct(name):
     d = _load(f"mol_{name}.npz")
     mol = _mol(d)
     E = mol.RHF(doPrint=False, direct=True)
-    assert abs(E - float(d["energy_direct"])) < 1e-8, (E, float(d["energy_direct"]))
+    assert abs(E - float(d["energy_direct"])) < 5e-8, (E, float(d["energy_direct"]))  # see above
     assert mol.is_converged
     # converged as far as the incremental build allows (the acc2e = 1e-12 screening of
     # every build leaves a ||dP|| floor near 1e-11, for the reference as for this
@@ -256,3 +258,32 @@ def test_mixed_precision_fock_and_energy():
     G64 = ctx.fock(P, tol=1e-12).clone()
     G32 = ctx.fock(P, tol=1e-12, fp32_below=1e-5)
     assert torch.max(torch.abs(G64 - G32)).item() < 1e-9
+
+
+def test_primitive_pair_screening_is_below_the_parity_tolerance():
+    """Contexts built with the default primitive-pair screening (1e-18) and with none
+    (prim_tol = 0) give the same Fock builds and ERI tensors to far below 1e-12, with
+    the same screened function quartets and fewer primitive quartets."""
+    import torch
+    from mmd import _native
+    from mmd.clusters import water_cluster
+    from mmd.integrals.shells import shells_from_bfs
+    from mmd.molecule import Molecule
+    m = Molecule(water_cluster(4, seed=3), "6-31gss")
+    ss = shells_from_bfs(m.bfs)
+    full, pruned = _native.Context(ss, prim_tol=0.0), _native.Context(ss)
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((m.nbasis, m.nbasis)) * 0.1
+    dP = torch.as_tensor(A + A.T, device="cuda").reshape(-1).contiguous()
+    G0 = full.fock(dP, counts=True).cpu().numpy()
+    c0 = full.last_counts.astype(np.int64)
+    G1 = pruned.fock(dP, counts=True).cpu().numpy()
+    c1 = pruned.last_counts.astype(np.int64)
+    assert np.abs(G1 - G0).max() < 1e-13
+    assert (c1[:, 0] == c0[:, 0]).all() and (c1[:, 1] == c0[:, 1]).all()
+    assert c1[:, 2].sum() < 0.95 * c0[:, 2].sum()
+    w = _mol(_load("mol_water_631gss.npz"))
+    ws = shells_from_bfs(w.bfs)
+    T0 = _native.Context(ws, prim_tol=0.0).eri_tensor().cpu().numpy()
+    T1 = _native.Context(ws).eri_tensor().cpu().numpy()
+    assert np.abs(T1 - T0).max() < 1e-14

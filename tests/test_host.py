@@ -119,3 +119,11 @@ def test_boys_table_vs_mpmath(built_lib):
                 assert abs(got - float(ex)) <= 1.2e-16 * abs(float(ex)), (k, L, nn)
         e = tab[ngrid * (lmax + 1) * row + k * row]
         assert abs(e - float(mp.exp(-T))) <= 1.2e-16 * float(mp.exp(-T))
+
+
+def test_realtime_rejects_unknown_direction():
+    from mmd.realtime import _axis
+    assert [_axis(d) for d in "xYz"] == [0, 1, 2]
+    import pytest as _pt
+    with _pt.raises(ValueError):
+        _axis("w")
