@@ -51,7 +51,7 @@ FQ_PER_BUILD = 198282802.0
 # DRAM bytes (read + write) of one launch of the top class kernels in the first, full
 # Fock build of this workload, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum; summary and command in profiles/k_fock_fp64_pipe_h2o16.md).
-DRAM_BYTES_PER_LAUNCH = {"1000": 48.3e6, "0000": 24.2e6, "1010": 25.6e6, "1110": 16.2e6, "2111": 5.5e6}
+DRAM_BYTES_PER_LAUNCH = {"1000": 47.7e6, "0000": 24.2e6, "1010": 25.5e6, "1110": 16.2e6, "2111": 5.3e6}
 
 
 def _env():
@@ -402,6 +402,47 @@ def combined_bench(nmol=64, thr=1e-5, conver=1e-8):
     return out
 
 
+def consumers_bench():
+    """Wall times of the reference's consumers of the hot path on the GPU path:
+    analytic forces (water 6-31G* distorted, (H2O)3 6-31G**), AO->MO + MP2
+    ((H2O)4 6-31G), RT-TDHF Magnus4 steps (water 6-31G)."""
+    import numpy as np
+    import torch
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    from mmd.postscf import PostSCF
+    from mmd.realtime import RealTime
+    bent = "\n0 1\nO 0.0 -0.07 0.01\nH 0.80 0.62 0.03\nH -0.88 0.56 -0.02\n"
+    out = {}
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    for name, geom, basis in (("water_distorted", bent, "6-31gs"), ("(H2O)3", water_cluster(3, seed=4), "6-31gss")):
+        mol = Molecule(geom, basis)
+        mol.RHF(doPrint=False, conver=1e-10)
+        mol.forces()  # warm
+        t, _ = timed(mol.forces)
+        out[f"forces_{name}_{basis}"] = {"s": t, "nbasis": int(mol.nbasis), "atoms": len(mol.atoms)}
+    mol = Molecule(water_cluster(4, seed=4), "6-31g")
+    mol.RHF(doPrint=False, conver=1e-10)
+    t, _ = timed(lambda: PostSCF(mol).MP2())
+    out["ao2mo_mp2_(H2O)4_6-31g"] = {"s": t, "nbasis": int(mol.nbasis)}
+    mol = Molecule(bent, "6-31g")
+
+    def pulse(t):
+        return np.exp(-((t - 1.0) ** 2) / 0.25)
+
+    rt = RealTime(mol, numsteps=100, stepsize=0.1, field=1e-3, pulse=pulse)
+    t, _ = timed(lambda: rt.Magnus4(direction="x"))
+    out["rt_magnus4_water_6-31g"] = {"s_per_step": t / 100, "steps": 100, "nbasis": int(mol.nbasis)}
+    return out
+
+
 # ------------------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import numpy as np
@@ -534,6 +575,12 @@ def gpu_arm(args):
             mixed = mixed_bench()
         except Exception as e:
             mixed = {"error": str(e)[:300]}
+    consumers = None
+    if rank == 0 and args.consumers:
+        try:
+            consumers = consumers_bench()
+        except Exception as e:
+            consumers = {"error": str(e)[:300]}
     if rank == 0 and not args.no_combined:
         try:
             combined = combined_bench()
@@ -551,7 +598,7 @@ def gpu_arm(args):
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches_per_build * builds, "wall_s": wall,
         "step_breakdown_ms": {"fock_build_kernels": build_ms, "rest_of_step": step_other_ms},
-        "batched": batched, "mixed_precision": mixed, "combined_form": combined,
+        "batched": batched, "mixed_precision": mixed, "combined_form": combined, "consumers": consumers,
         "class_ms_per_build": {"%d%d%d%d" % c: float(x) / builds for c, x in zip(flop_model.CLASSES, class_ms)},
         "class_counts_per_build": {"%d%d%d%d" % c: [float(v) / builds for v in row]
                                    for c, row in zip(flop_model.CLASSES, counts)},
@@ -595,6 +642,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-molecule batched sub-benchmark")
     ap.add_argument("--no-mixed", action="store_true", help="skip the (H2O)32 mixed-precision sub-benchmark")
     ap.add_argument("--no-combined", action="store_true", help="skip the learned+batched+mixed sub-benchmark")
+    ap.add_argument("--consumers", action="store_true", help="also time forces, MP2 and RT-TDHF")
     ap.add_argument("--n-water", type=int, default=16, help="cluster size (16 = the benchmark workload)")
     ap.add_argument("--cpu-sample", metavar="SPEC")
     ap.add_argument("--cores", type=int, default=None)

@@ -195,11 +195,11 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
         o.append(f"      for (int i = c.bra_begin; i < c.bra_end; ++i) {{")
         for fcd in ch:
             o.append("        Real " + ", ".join(f"w{fcd}_{k} = 0" for k in range(len(hp))) + ";")
+        o.append(f"        const auto ap = c.pp(i);")
+        o.append(f"        auto bq = c.pp(c.ket_begin);")
         if not smem and L <= UNROLL_KET_MAX_L:
             # two independent primitive quartets in flight: hides the Boys/rsqrt chains
             o.append(f"#pragma unroll 2")
-        o.append(f"        const auto ap = c.pp(i);")
-        o.append(f"        auto bq = c.pp(c.ket_begin);")
         o.append(f"        for (int j = c.ket_begin; j < c.ket_end; ++j) {{")
         o.append(f"          const auto bp = bq;")
         o.append(f"          if (j + 1 < c.ket_end) bq = c.pp(j + 1);  // next ket primitive pair, one iteration ahead")

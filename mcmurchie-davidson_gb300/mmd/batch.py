@@ -26,6 +26,44 @@ from .molecule import Molecule
 from .scf import diis_error_growing
 
 
+def _openblas_controls():
+    """(get, set) thread-count functions of the OpenBLAS that numpy loaded, or None."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = sorted({ln.split()[-1] for ln in f if "openblas" in ln.lower() and ln.split()[-1].startswith("/")})
+    except OSError:
+        return None
+    for path in paths:
+        try:
+            lib = ctypes.CDLL(path)
+        except OSError:
+            continue
+        for pre, suf in (("scipy_openblas", "64_"), ("scipy_openblas", ""), ("openblas", "64_"), ("openblas", "")):
+            g, s = f"{pre}_get_num_threads{suf}", f"{pre}_set_num_threads{suf}"
+            if hasattr(lib, g) and hasattr(lib, s):
+                get, set_ = getattr(lib, g), getattr(lib, s)
+                get.restype = ctypes.c_int
+                set_.argtypes = [ctypes.c_int]
+                return get, set_
+    return None
+
+
+class _single_threaded_blas:
+    """Context manager: numpy's OpenBLAS on one thread (no-op if it cannot be found)."""
+
+    def __enter__(self):
+        self.ctl = _openblas_controls()
+        if self.ctl:
+            self.prev = self.ctl[0]()
+            self.ctl[1](1)
+        return self
+
+    def __exit__(self, *exc):
+        if self.ctl:
+            self.ctl[1](self.prev)
+        return False
+
+
 class BatchRHF:
     def __init__(self, geometries, basis="6-31g", acc2e=1e-12, fp32_below=0.0, graph=True, tuning=None):
         torch = _native._torch()
@@ -126,7 +164,12 @@ class BatchRHF:
             self.ctx.fock(self._dP_buf, self._G_buf, tol=self.acc2e, fp32_below=self.fp32_below)
         return self._G_buf
 
-    def _eigh(self, FO):
+    def _eigh(self, FO, active=None):
+        """Eigenpairs of every (active) molecule's block, on the host cores: one LAPACK
+        call per molecule in a thread pool, with numpy's OpenBLAS held to one thread
+        meanwhile (16 solves in parallel beat 16 threads inside each small solve:
+        0.13 s against 0.45 s for 1024 matrices of 13..104 on the Grace host).
+        Converged (inactive) molecules are skipped; their slots return zeros."""
         FOh = FO.cpu().numpy()
         E = np.zeros((self.B, self.Nmax))
         C = np.zeros_like(FOh)
@@ -137,8 +180,9 @@ class BatchRHF:
             E[b, :n] = w
             C[b, :n, :n] = v
 
-        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
-            list(ex.map(one, range(self.B)))
+        todo = range(self.B) if active is None else np.flatnonzero(active)
+        with _single_threaded_blas(), ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            list(ex.map(one, todo))
         return self.torch.as_tensor(E, device=self.dev), self.torch.as_tensor(C, device=self.dev)
 
     def _density(self, CO):
@@ -248,7 +292,7 @@ class BatchRHF:
             else:
                 FO = X.transpose(1, 2) @ F @ X
             FO = FO + torch.diag_embed(self.pad_shift)
-            _, CO = self._eigh(FO)
+            _, CO = self._eigh(FO, ~done)
             Pn = self._density(CO)
             P = torch.where(active, Pn, P)
             e = (torch.sum((Core + F) * P.transpose(1, 2), dim=(1, 2))).cpu().numpy() + self.nuc

@@ -98,6 +98,20 @@ class Molecule(SCF, Forces):
     """Molecule with GPU integrals (mmd/molecule.py:24-315)."""
 
     @property
+    def double_bar(self):
+        """Spin-orbital <AB||CD> set up by PostSCF(mol), built on first access."""
+        if getattr(self, "_double_bar", None) is None:
+            build = getattr(self, "_double_bar_build", None)
+            if build is None:
+                raise AttributeError("double_bar: run PostSCF(mol) first")
+            self._double_bar = build()
+        return self._double_bar
+
+    @double_bar.setter
+    def double_bar(self, value):
+        self._double_bar = value
+
+    @property
     def _forces(self):
         """Forces of every atom, natom x 3 (mmd/molecule.py:47-53)."""
         return np.concatenate([atom.forces for atom in self.atoms]).reshape(-1, 3)

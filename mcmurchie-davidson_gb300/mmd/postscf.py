@@ -5,9 +5,9 @@
 runs ``ao2mo``: the 4-index transform (pq|rs) -> (PQ|RS) as four FP64 contractions
 over one index each (cuBLAS DGEMMs through torch: plain library GEMMs), the
 spin-orbital antisymmetrised integrals <AB||CD> (spin orbital 2p + sigma, the
-ordering of the reference's Kronecker products), the spin-orbital core Hamiltonian
-``Hp`` and orbital energies ``fs`` -- the attributes the reference sets, as host
-arrays.  ``MP2`` evaluates the reference's sums (spatial, and spin-orbital from
+ordering of the reference's Kronecker products; built on first use), the spin-orbital
+core Hamiltonian ``Hp`` and orbital energies ``fs`` -- the attributes the reference
+sets, as host arrays.  ``MP2`` evaluates the reference's sums (spatial, and spin-orbital from
 <ij||ab>) as vectorised device reductions instead of Python loops.
 
 The reference's configuration-interaction and response methods (CIS, CISD, FCI,
@@ -19,9 +19,6 @@ from __future__ import annotations
 import sys
 
 import numpy as np
-
-# host copies of the (2N)^4 spin-orbital tensor are made up to this many elements
-HOST_DOUBLE_BAR_MAX = 1 << 28
 
 
 class PostSCF:
@@ -54,20 +51,41 @@ class PostSCF:
         self._mo = mo
         mol.single_bar = mo.cpu().numpy()
         mol.norb = 2 * N
-        # spin-orbital <AB||CD> with A = 2a + sigma: <AB|CD> = (ac|bd) d(sA,sC) d(sB,sD)
-        spin = torch.arange(2 * N, device=dev) % 2
-        sp = torch.arange(2 * N, device=dev) // 2
-        same = (spin[:, None] == spin[None, :]).to(torch.float64)
-        phys = mo.permute(0, 2, 1, 3)                                    # <ab|cd> = (ac|bd)
-        big = phys[sp][:, sp][:, :, sp][:, :, :, sp]                     # <AB|CD> without spin
-        direct = big * same[:, None, :, None] * same[None, :, None, :]   # d(sA,sC) d(sB,sD)
-        self._double_bar = direct - direct.permute(0, 1, 3, 2)
-        if self._double_bar.numel() <= HOST_DOUBLE_BAR_MAX:
-            mol.double_bar = self._double_bar.cpu().numpy()
+        # the (2N)^4 spin-orbital tensor is built when first used (MP2(spin_orbital=True)
+        # or mol.double_bar), not here: it is 16x the spatial one
+        self._double_bar = None
+        mol._double_bar = None
+        mol._double_bar_build = lambda: self._spin_tensor().cpu().numpy()
         Core = mol._dev["Core"]
         h = C.T @ Core @ C
         mol.Hp = np.kron(h.cpu().numpy(), np.eye(2))
         mol.fs = np.kron(np.diag(np.real(np.asarray(mol.MO))), np.eye(2))
+
+    def _spin_block(self, A, B, C, D):
+        """Block <AB||CD> of the spin-orbital integrals for index ranges A..D (spin
+        orbital 2p + sigma, mmd/postscf.py:31-35): <AB|CD> = (ac|bd) d(sA,sC) d(sB,sD),
+        antisymmetrised in C, D."""
+        torch = self.mol.context.torch
+        dev = self._mo.device
+        idx = [torch.arange(r.start, r.stop, device=dev) for r in (A, B, C, D)]
+        sp = [i // 2 for i in idx]
+        sg = [i % 2 for i in idx]
+        phys = self._mo.permute(0, 2, 1, 3)                             # <ab|cd> = (ac|bd)
+
+        def coulomb(c, d):
+            blk = phys[sp[0]][:, sp[1]][:, :, sp[c]][:, :, :, sp[d]]
+            s_ac = (sg[0][:, None] == sg[c][None, :]).to(blk.dtype)
+            s_bd = (sg[1][:, None] == sg[d][None, :]).to(blk.dtype)
+            return blk * s_ac[:, None, :, None] * s_bd[None, :, None, :]
+
+        return coulomb(2, 3) - coulomb(3, 2).permute(0, 1, 3, 2)
+
+    def _spin_tensor(self):
+        """The whole (2N)^4 spin-orbital tensor (device, cached)."""
+        if self._double_bar is None:
+            n = range(0, 2 * self._mo.shape[0])
+            self._double_bar = self._spin_block(n, n, n, n)
+        return self._double_bar
 
     def MP2(self, spin_orbital=False):
         """MP2 energy from the RHF reference (mmd/postscf.py:44-73)."""
@@ -78,7 +96,8 @@ class PostSCF:
             e = torch.as_tensor(np.diag(mol.fs).copy(), dtype=torch.float64, device=dev)
             o, v = slice(0, mol.nelec), slice(mol.nelec, mol.norb)
             d = e[o][:, None, None, None] + e[o][None, :, None, None] - e[v][None, None, :, None] - e[v][None, None, None, :]
-            num = self._double_bar[o, o, v, v] ** 2
+            num = self._spin_block(range(o.start, o.stop), range(o.start, o.stop), range(v.start, v.stop),
+                                   range(v.start, v.stop)) ** 2
             mol.emp2 = np.complex128(0.25 * float((num / d).sum().item()) + mol.energy)
         else:
             e = torch.as_tensor(np.real(np.asarray(mol.MO)), dtype=torch.float64, device=dev)

@@ -127,3 +127,18 @@ def test_realtime_rejects_unknown_direction():
     import pytest as _pt
     with _pt.raises(ValueError):
         _axis("w")
+
+
+def test_single_threaded_blas_scope_restores_the_thread_count():
+    import numpy as np
+    from mmd.batch import _openblas_controls, _single_threaded_blas
+    ctl = _openblas_controls()
+    if ctl is None:
+        import pytest as _pt
+        _pt.skip("numpy's OpenBLAS not found in this process")
+    before = ctl[0]()
+    with _single_threaded_blas():
+        assert ctl[0]() == 1
+        w = np.linalg.eigh(np.diag([3.0, 1.0, 2.0]))[0]
+    assert ctl[0]() == before
+    assert w.tolist() == [1.0, 2.0, 3.0]
