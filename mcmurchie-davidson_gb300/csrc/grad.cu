@@ -138,9 +138,12 @@ __device__ void hermite_r(int M, double alpha, double X, double Y, double Z, con
 }
 
 // ------------------------------------------------------------------ one-electron terms
+// One thread per (shell pair, nucleus): the nucleus' attraction terms, and for
+// nucleus 0 also the overlap and kinetic terms of the pair.
 __global__ void k_grad_one(GradArgs a) {
-  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pr >= a.npair) return;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (tid >= (long long)a.npair * a.natom) return;
+  const int pr = (int)(tid / a.natom), cnuc = (int)(tid - (long long)pr * a.natom);
   const int sa = a.pa[pr], sb = a.pb[pr];
   const int la = a.L[sa], lb = a.L[sb];
   const int Ka = a.nprim[sa], Kb = a.nprim[sb];
@@ -153,7 +156,7 @@ __global__ void k_grad_one(GradArgs a) {
   E1 E[3];
   double R[kRsize], F[kLtot + 2];
   // ---- overlap and kinetic: d/dB = -d/dA
-  for (int ka = 0; ka < Ka; ++ka)
+  for (int ka = 0; ka < (cnuc == 0 ? Ka : 0); ++ka)
     for (int kb = 0; kb < Kb; ++kb) {
       const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
       const double p = ea + eb, mu = ea * eb / p;
@@ -204,13 +207,15 @@ __global__ void k_grad_one(GradArgs a) {
         }
       }
     }
-  for (int d = 0; d < 3; ++d) {
-    atomicAdd(a.grad + 3 * atA + d, gA[d]);
-    atomicAdd(a.grad + 3 * atB + d, -gA[d]);
-  }
-  // ---- nuclear attraction, one nucleus at a time: basis terms on A and B, and the
+  if (cnuc == 0)
+    for (int d = 0; d < 3; ++d) {
+      atomicAdd(a.grad + 3 * atA + d, gA[d]);
+      atomicAdd(a.grad + 3 * atB + d, -gA[d]);
+    }
+  // ---- nuclear attraction of this thread's nucleus: basis terms on A and B, and the
   // Hellmann-Feynman term on the nucleus, -(A + B)
-  for (int c = 0; c < a.natom; ++c) {
+  {
+    const int c = cnuc;
     const double C[3] = {a.xyz[3 * c], a.xyz[3 * c + 1], a.xyz[3 * c + 2]};
     const double Zc = a.Z[c];
     double vA[3] = {0, 0, 0}, vB[3] = {0, 0, 0};
@@ -279,7 +284,9 @@ __global__ void k_grad_one(GradArgs a) {
 // factor 2 P_ij P_kl - (P_ik P_jl + P_il P_jk) / 2 (the exchange term averaged over the
 // quartet's permutations).
 __global__ void k_grad_two(GradArgs a) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // a warp per shell quartet; its lanes split the bra component pairs
+  const long long q = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   const long long nq = (long long)a.npair * (a.npair + 1) / 2;
   if (q >= nq) return;
   // (ip, iq) from the triangular index q = ip (ip + 1) / 2 + iq
@@ -334,8 +341,9 @@ __global__ void k_grad_two(GradArgs a) {
           boys_series(M, alpha * (X * X + Y * Y + Z * Z), F);
           hermite_r(M, alpha, X, Y, Z, F, R);
           const double pref = 2.0 * pow(kPi, 2.5) / (p * qq * sqrt(p + qq)) * Kab * Kcd;
-          for (int ca = 0; ca < nc[0]; ++ca)
-            for (int cb = 0; cb < nc[1]; ++cb) {
+          for (int cab = lane; cab < nc[0] * nc[1]; cab += 32) {
+            {
+              const int ca = cab / nc[1], cb = cab - (cab / nc[1]) * nc[1];
               if (same_ab && ca < cb) continue;
               const int fi0 = a.func[s[0] * kGradMaxComp + ca], fj0 = a.func[s[1] * kGradMaxComp + cb];
               if (fi0 < 0 || fj0 < 0) continue;
@@ -450,8 +458,13 @@ __global__ void k_grad_two(GradArgs a) {
                   }
                 }
             }
+          }
         }
     }
+  for (int x = 0; x < 3; ++x)
+    for (int d = 0; d < 3; ++d)
+      for (int o = 16; o > 0; o >>= 1) g[x][d] += __shfl_xor_sync(0xffffffffu, g[x][d], o);
+  if (lane != 0) return;
   const int at[4] = {a.shell_atom[s[0]], a.shell_atom[s[1]], a.shell_atom[s[2]], a.shell_atom[s[3]]};
   for (int d = 0; d < 3; ++d) {
     atomicAdd(a.grad + 3 * at[0] + d, g[0][d]);
@@ -465,10 +478,11 @@ __global__ void k_grad_two(GradArgs a) {
 
 cudaError_t mmdg_launch_rhf_gradient(const GradArgs& a, cudaStream_t st) {
   if (a.npair <= 0) return cudaSuccess;
-  k_grad_one<<<(a.npair + 63) / 64, 64, 0, st>>>(a);
+  const long long n1 = (long long)a.npair * a.natom;
+  k_grad_one<<<(unsigned)((n1 + 63) / 64), 64, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const long long nq = (long long)a.npair * (a.npair + 1) / 2;
-  k_grad_two<<<(unsigned)((nq + 63) / 64), 64, 0, st>>>(a);
+  k_grad_two<<<(unsigned)((nq * 32 + 127) / 128), 128, 0, st>>>(a);
   return cudaGetLastError();
 }

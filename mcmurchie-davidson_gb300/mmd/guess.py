@@ -310,6 +310,45 @@ def train(features, targets, masks, epochs=30, batch=8192, lr=2e-3, seed=0, log=
 
 
 def predict_density(net, mol):
+    """Initial density of ``mol``.  A 6-31G molecule is predicted directly; a basis
+    that contains 6-31G (6-31G*, 6-31G**: the same s and p functions first on every
+    atom, polarisation functions after them) gets the 6-31G prediction embedded, zero
+    on the polarisation functions.  The embedded matrix is a valid density of the
+    larger basis (P S P = P and tr(P S) = N/2 hold on the shared functions)."""
+    try:
+        Z, _, _ = molecule_layout(mol)
+    except ValueError:
+        return _embedded_prediction(net, mol)
     pairs, F, _, _, (Z, R, off) = molecule_samples(mol)
     pred = net.predict(net.torch.tensor(F, device="cuda")).cpu().numpy()
     return assemble(pred, Z, R, off, pairs, mol.nbasis)
+
+
+def _embedded_prediction(net, mol):
+    from .molecule import Molecule
+    small = Molecule(mol.geometry_input, "6-31g")
+    return embed_density(small, mol, predict_density(net, small))
+
+
+def embed_density(small, mol, Ps):
+    """Ps of the 6-31G molecule ``small`` placed on the matching functions of ``mol``
+    (same geometry, a basis whose first functions on every atom are 6-31G's)."""
+    big_of_atom, small_of_atom = {}, {}
+    for k, a in enumerate(mol.bf_atom):
+        big_of_atom.setdefault(a, []).append(k)
+    for k, a in enumerate(small.bf_atom):
+        small_of_atom.setdefault(a, []).append(k)
+    idx = np.empty(small.nbasis, dtype=np.int64)
+    for a, ks in small_of_atom.items():
+        kb = big_of_atom.get(a, [])[:len(ks)]
+        if len(kb) != len(ks):
+            raise ValueError("the basis does not contain 6-31G")
+        for i, j in zip(ks, kb):
+            bs, bb = small.bfs[i], mol.bfs[j]
+            if (tuple(np.asarray(bs.shell)) != tuple(np.asarray(bb.shell))
+                    or not np.allclose(np.asarray(bs.exps)[:bs.num_exps], np.asarray(bb.exps)[:bb.num_exps])):
+                raise ValueError("the basis does not contain 6-31G")
+            idx[i] = j
+    P = np.zeros((mol.nbasis, mol.nbasis))
+    P[np.ix_(idx, idx)] = Ps
+    return P

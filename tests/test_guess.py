@@ -151,3 +151,46 @@ def test_guess_fallback_restart_reaches_core_energy(monkeypatch):
     assert br.reverted.tolist() == [True, False]
     assert br.converged.all()
     assert np.abs(E - Ec).max() < 1e-9
+
+
+@pytest.mark.gpu
+def test_embedded_guess_for_631gss_converges_faster_to_the_same_energy():
+    """The 6-31G network's prediction embedded in 6-31G** (polarisation functions
+    zero) is a valid density there, cuts the direct SCF iterations of a held-out
+    (H2O)8, and the polished energies agree with the core-guess run."""
+    from mmd import guess as G
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    net = G.DensityMLP.load()
+    geom = water_cluster(8, seed=900123)
+    m = Molecule(geom, "6-31gss")
+    P0 = G.predict_density(net, m)
+    assert P0.shape == (m.nbasis, m.nbasis)
+    core = Molecule(geom, "6-31gss")
+    Ec = core.RHF(doPrint=False, direct=True, conver=1e-9, polish=True)
+    learned = Molecule(geom, "6-31gss")
+    El = learned.RHF(doPrint=False, direct=True, conver=1e-9, guess=P0, polish=True)
+    assert abs(np.trace(P0 @ learned.S) - learned.nocc) < 0.05 * learned.nocc
+    assert not learned.guess_reverted
+    assert learned.iterations < core.iterations
+    assert abs(El - Ec) < 1e-9
+
+
+def test_embedding_places_631g_blocks_on_the_shared_functions():
+    from mmd import guess as G
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    geom = water_cluster(2, seed=3)
+    small, big = Molecule(geom, "6-31g"), Molecule(geom, "6-31gss")
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((small.nbasis, small.nbasis))
+    Ps = A + A.T
+    P = G.embed_density(small, big, Ps)
+    keep = [k for k, b in enumerate(big.bfs) if sum(int(x) for x in b.shell) <= 1 and
+            not (big.atoms[big.bf_atom[k]].charge == 1 and sum(int(x) for x in b.shell) == 1)]
+    assert len(keep) == small.nbasis
+    assert np.array_equal(P[np.ix_(keep, keep)], Ps)
+    rest = np.setdiff1d(np.arange(big.nbasis), keep)
+    assert not P[rest].any() and not P[:, rest].any()
+    with pytest.raises(ValueError):
+        G.embed_density(small, Molecule(geom, "sto-3g"), Ps)
