@@ -178,7 +178,6 @@ def gen_class(la, lb, lc, ld, chunk=None, smem=None, compact=None):
     o.append(f"  static constexpr int NAB = {nab}, NCD = {ncd}, NNZ_AB = {nnz_ab}, NNZ_CD = {nnz_cd};")
     nchunk = -(-ncd // chunk)
     o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = {chunk}, NCHUNK = {nchunk}, RSMEM = {smem};")
-    o.append(f"  static constexpr int MINB = {MIN_BLOCKS.get((la, lb, lc, ld), 1)};")
     o.append(f"  template <class Ctx, class Digest>")
     o.append(f"  static __device__ __forceinline__ void run(const Ctx& c, Digest& dg) {{")
     if smem:
@@ -273,7 +272,6 @@ def gen_class_compact(la, lb, lc, ld):
     o.append(f"  static constexpr int LA = {la}, LB = {lb}, LC = {lc}, LD = {ld}, L = {L};")
     o.append(f"  static constexpr int NAB = {nab}, NCD = {ncd}, NNZ_AB = {nnz_ab}, NNZ_CD = {nnz_cd};")
     o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)}, CHUNK = 1, NCHUNK = {ncd}, RSMEM = 1;")
-    o.append(f"  static constexpr int MINB = 1;")
     o.append(f"  template <class Ctx, class Digest>")
     o.append(f"  static __device__ __forceinline__ void run(const Ctx& c, Digest& dg) {{")
     o.append(f"    Real* __restrict__ Rs = c.template rsmem<Real>();")
@@ -326,9 +324,6 @@ def gen_class_compact(la, lb, lc, ld):
 COMPACT_ABOVE_L = 4
 # register-resident classes up to this total L unroll the ket primitive loop by two
 UNROLL_KET_MAX_L = 2
-# Blocks of 128 threads each SM must be able to hold for the class kernel (register cap
-# 65536 / (128 MINB)): the low-L classes are latency bound with few resident warps.
-MIN_BLOCKS = {(0, 0, 0, 0): 8, (1, 0, 0, 0): 6, (1, 0, 1, 0): 5, (1, 1, 0, 0): 5}
 
 
 def generate(path, overrides=None):

@@ -120,7 +120,7 @@ constexpr int kMaxKeys = 256;
 // (chunk, bucket, quartet), chunk-major, so that a warp shares its chunk (code
 // path) and, inside a bucket, its primitive trip counts.
 template <class MD, typename Real>
-__global__ void __launch_bounds__(kThreads, MD::MINB) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
+__global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
                                                    const unsigned* count, const long long* key_off, int nkeys) {
   __shared__ unsigned s_pre[kMaxKeys + 1];
   __shared__ long long s_off[kMaxKeys];
