@@ -448,7 +448,7 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=1e-5):
     from mmd.integrals import twoe
     from mmd.molecule import Molecule
     E_oracle = plain_mol.polished_energy()
-    net = G.DensityMLP.load()
+    net = G.network_for(Molecule(geom, "6-31gss"))
     twoe._ctx_cache.clear()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -457,8 +457,10 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=1e-5):
     E = float(m.RHF(doPrint=False, direct=True, fp32_below=thr, guess=P0, polish=True))
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
-    return {"form": "learned guess + FP32 below %g + FP64 polish" % thr, "time_to_converge_s": t,
+    return {"form": "learned guess + FP32 below %g + FP64 polish" % thr, "network": net.gb.name,
+            "time_to_converge_s": t,
             "iterations": int(m.iterations), "guess_reverted": bool(m.guess_reverted),
+            "iterations_s": float(m.scf_time), "plain_iterations_s": float(plain_mol.scf_time),
             "speedup_vs_plain_fp64": ttc_plain / t, "plain_fp64_iterations": iters_plain,
             "energy": E, "energy_error_vs_fp64_oracle": E - E_oracle,
             "plain_fp64_energy_error_vs_oracle": float(plain_mol.energy) - E_oracle}

@@ -22,6 +22,12 @@ a mask.
 
 The network: 53 -> 256 -> 256 -> 81, SiLU, BF16 weights with FP32 accumulation,
 trained with Adam on the GPU by the kernels of csrc/mlp.cu (``mmdg_mlp_*``).
+
+The same construction covers 6-31G** (``B631GSS``: O has 15 functions with the d
+sextet, H has 5 with a p triplet; blocks padded to 15 x 15, 225 outputs).  Cartesian
+d functions rotate as quadratic monomials (``d_transform``), a non-orthogonal
+transform, so a block goes to the local frames as T_A^-T P[A,B] T_B^-1 and back as
+T_A^T P' T_B.
 """
 from __future__ import annotations
 
@@ -40,7 +46,27 @@ TYPES = {(8, 8): 0, (8, 1): 1, (1, 8): 2, (1, 1): 3}
 RBF_CENTERS = np.linspace(0.5, 8.0, 32) / ANG
 RBF_WIDTH = 0.24 / ANG
 CUTOFF = 8.0 / ANG
-WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "guess_mlp_631g.npz")
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+WEIGHTS = os.path.join(DATA, "guess_mlp_631g.npz")
+
+
+class GuessBasis:
+    """Function layout a network predicts: the shells of each element in basis order
+    ('S', 'P', 'D'), the block padding and the weights file."""
+
+    def __init__(self, name, shells, weights):
+        self.name = name
+        self.shells = shells
+        self.nfunc = {z: sum({"S": 1, "P": 3, "D": 6}[c] for c in sh) for z, sh in shells.items()}
+        self.nmax = max(self.nfunc.values())
+        self.nout = self.nmax * self.nmax
+        self.weights = weights
+        self.has_d = any("D" in sh for sh in shells.values())
+
+
+B631G = GuessBasis("6-31g", {8: "SSPSP", 1: "SS"}, WEIGHTS)
+B631GSS = GuessBasis("6-31gss", {8: "SSPSPD", 1: "SSP"}, os.path.join(DATA, "guess_mlp_631gss.npz"))
+BASES = {"6-31g": B631G, "6-31gss": B631GSS}
 
 
 # ---------------------------------------------------------------- geometry
@@ -70,20 +96,50 @@ def atom_frames(coords: np.ndarray) -> np.ndarray:
     return R
 
 
-def block_transform(Z: int, R: np.ndarray) -> np.ndarray:
-    T = np.eye(NFUNC[Z])
-    for p in PTRIPLETS[Z]:
-        T[p:p + 3, p:p + 3] = R
+_DPAIRS = ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))  # xx xy xz yy yz zz
+_DNORM = np.array([1.0 / np.sqrt(3.0), 1.0, 1.0, 1.0 / np.sqrt(3.0), 1.0, 1.0 / np.sqrt(3.0)])
+
+
+def d_transform(R: np.ndarray) -> np.ndarray:
+    """Cartesian d functions n_ab x_a x_b in the frame x' = R x: phi' = T phi with
+    T[ab, kl] = n_ab / n_kl (R_ak R_bl + R_al R_bk) (k < l) or n_ab / n_kk R_ak R_bk."""
+    T = np.zeros((6, 6))
+    for i, (a, b) in enumerate(_DPAIRS):
+        for j, (k, l) in enumerate(_DPAIRS):
+            c = R[a, k] * R[b, l] + (R[a, l] * R[b, k] if k != l else 0.0)
+            T[i, j] = _DNORM[i] / _DNORM[j] * c
     return T
 
 
-def molecule_layout(mol):
+def block_transform(Z: int, R: np.ndarray, gb: GuessBasis = B631G) -> np.ndarray:
+    """Functions of an atom in its local frame, phi' = T phi (s unchanged, p triplets
+    rotated by R, d sextets by d_transform)."""
+    T = np.eye(gb.nfunc[Z])
+    o = 0
+    for c in gb.shells[Z]:
+        if c == "P":
+            T[o:o + 3, o:o + 3] = R
+        elif c == "D":
+            T[o:o + 6, o:o + 6] = d_transform(R)
+        o += {"S": 1, "P": 3, "D": 6}[c]
+    return T
+
+
+def _to_local(T):
+    """Density-block transform to the local functions: P' = T^-T P T^-1 (= T P T^T for
+    the orthogonal s/p transform)."""
+    return np.linalg.inv(T).T
+
+
+def molecule_layout(mol, gb: GuessBasis = B631G):
     """Atomic numbers, coordinates (bohr) and first-function offsets of a Molecule."""
     Z = np.array([a.charge for a in mol.atoms])
     X = np.array([a.origin for a in mol.atoms])
-    off = np.concatenate([[0], np.cumsum([NFUNC[int(z)] for z in Z])[:-1]])
-    if off[-1] + NFUNC[int(Z[-1])] != mol.nbasis:
-        raise ValueError("the learned guess covers H and O in 6-31G only")
+    if any(int(z) not in gb.nfunc for z in Z):
+        raise ValueError(f"the learned guess covers H and O in {gb.name} only")
+    off = np.concatenate([[0], np.cumsum([gb.nfunc[int(z)] for z in Z])[:-1]])
+    if off[-1] + gb.nfunc[int(Z[-1])] != mol.nbasis:
+        raise ValueError(f"the learned guess covers H and O in {gb.name} only")
     return Z, X, off
 
 
@@ -111,15 +167,19 @@ def pair_features(Z, X, R):
     return pairs, np.array(rows, dtype=np.float32)
 
 
-def pair_targets(P, Z, R, off, pairs):
-    Y = np.zeros((len(pairs), NOUT), dtype=np.float32)
-    M = np.zeros((len(pairs), NOUT), dtype=np.float32)
+def pair_targets(P, Z, R, off, pairs, gb: GuessBasis = B631G):
+    nm = gb.nmax
+    Y = np.zeros((len(pairs), gb.nout), dtype=np.float32)
+    M = np.zeros((len(pairs), gb.nout), dtype=np.float32)
     for k, (a, b) in enumerate(pairs):
-        na, nb = NFUNC[int(Z[a])], NFUNC[int(Z[b])]
+        na, nb = gb.nfunc[int(Z[a])], gb.nfunc[int(Z[b])]
         blk = P[off[a]:off[a] + na, off[b]:off[b] + nb]
-        loc = block_transform(int(Z[a]), R[a]) @ blk @ block_transform(int(Z[b]), R[b]).T
-        t = np.zeros((9, 9))
-        m = np.zeros((9, 9))
+        Ta, Tb = block_transform(int(Z[a]), R[a], gb), block_transform(int(Z[b]), R[b], gb)
+        if gb.has_d:
+            Ta, Tb = _to_local(Ta), _to_local(Tb)
+        loc = Ta @ blk @ Tb.T
+        t = np.zeros((nm, nm))
+        m = np.zeros((nm, nm))
         t[:na, :nb] = loc
         m[:na, :nb] = 1.0
         Y[k] = t.ravel()
@@ -127,12 +187,13 @@ def pair_targets(P, Z, R, off, pairs):
     return Y, M
 
 
-def assemble(pred, Z, R, off, pairs, N):
+def assemble(pred, Z, R, off, pairs, N, gb: GuessBasis = B631G):
+    nm = gb.nmax
     P = np.zeros((N, N))
     for k, (a, b) in enumerate(pairs):
-        na, nb = NFUNC[int(Z[a])], NFUNC[int(Z[b])]
-        loc = pred[k].reshape(9, 9)[:na, :nb]
-        blk = block_transform(int(Z[a]), R[a]).T @ loc @ block_transform(int(Z[b]), R[b])
+        na, nb = gb.nfunc[int(Z[a])], gb.nfunc[int(Z[b])]
+        loc = pred[k].reshape(nm, nm)[:na, :nb]
+        blk = block_transform(int(Z[a]), R[a], gb).T @ loc @ block_transform(int(Z[b]), R[b], gb)
         if a == b:
             blk = 0.5 * (blk + blk.T)
         P[off[a]:off[a] + na, off[b]:off[b] + nb] = blk
@@ -141,13 +202,13 @@ def assemble(pred, Z, R, off, pairs, N):
     return P
 
 
-def molecule_samples(mol, P=None):
-    Z, X, off = molecule_layout(mol)
+def molecule_samples(mol, P=None, gb: GuessBasis = B631G):
+    Z, X, off = molecule_layout(mol, gb)
     R = atom_frames(X)
     pairs, F = pair_features(Z, X, R)
     if P is None:
         return pairs, F, None, None, (Z, R, off)
-    Y, M = pair_targets(np.asarray(P), Z, R, off, pairs)
+    Y, M = pair_targets(np.asarray(P), Z, R, off, pairs, gb)
     return pairs, F, Y, M, (Z, R, off)
 
 
@@ -155,15 +216,15 @@ def molecule_samples(mol, P=None):
 class DensityMLP:
     """53 -> 256 -> 256 -> 81 MLP; FP32 master weights, BF16 copies used by the kernels."""
 
-    def __init__(self, seed=0, weights=None):
+    def __init__(self, seed=0, weights=None, gb: GuessBasis = B631G):
         torch = _native._torch()
         self.torch = torch
         self.dev = "cuda"
-        _native.lib()
+        self.gb = gb
         L = _native.lib()
         self._sig(L)
         rng = np.random.default_rng(seed)
-        shapes = [(NHID, NIN), (NHID, NHID), (NOUT, NHID)]
+        shapes = [(NHID, NIN), (NHID, NHID), (gb.nout, NHID)]
         if weights is None:
             W = [rng.standard_normal(s) * np.sqrt(1.0 / s[1]) for s in shapes]
             b = [np.zeros(s[0]) for s in shapes]
@@ -271,18 +332,22 @@ class DensityMLP:
             out[f"b{i}"] = self.b[i].cpu().numpy()
         return out
 
-    def save(self, path=WEIGHTS):
+    def save(self, path=None):
+        path = path or self.gb.weights
         os.makedirs(os.path.dirname(path), exist_ok=True)
         np.savez_compressed(path, **self.state())
 
     @classmethod
     def load(cls, path=WEIGHTS):
-        return cls(weights=dict(np.load(path)))
+        w = dict(np.load(path))
+        nout = w["W2"].shape[0]
+        gb = next(b for b in BASES.values() if b.nout == nout)
+        return cls(weights=w, gb=gb)
 
 
-def train(features, targets, masks, epochs=30, batch=8192, lr=2e-3, seed=0, log=None):
+def train(features, targets, masks, epochs=30, batch=8192, lr=2e-3, seed=0, log=None, gb: GuessBasis = B631G):
     """Adam on masked MSE; features/targets/masks are float32 arrays (rows = pairs)."""
-    net = DensityMLP(seed=seed)
+    net = DensityMLP(seed=seed, gb=gb)
     torch = net.torch
     Xd = torch.tensor(features, device="cuda")
     Yd = torch.tensor(targets, device="cuda")
@@ -315,13 +380,29 @@ def predict_density(net, mol):
     atom, polarisation functions after them) gets the 6-31G prediction embedded, zero
     on the polarisation functions.  The embedded matrix is a valid density of the
     larger basis (P S P = P and tr(P S) = N/2 hold on the shared functions)."""
+    gb = getattr(net, "gb", B631G)
     try:
-        Z, _, _ = molecule_layout(mol)
+        molecule_layout(mol, gb)
     except ValueError:
+        if gb is not B631G:
+            raise
         return _embedded_prediction(net, mol)
-    pairs, F, _, _, (Z, R, off) = molecule_samples(mol)
+    pairs, F, _, _, (Z, R, off) = molecule_samples(mol, None, gb)
     pred = net.predict(net.torch.tensor(F, device="cuda")).cpu().numpy()
-    return assemble(pred, Z, R, off, pairs, mol.nbasis)
+    return assemble(pred, Z, R, off, pairs, mol.nbasis, gb)
+
+
+def network_for(mol):
+    """The committed network that covers ``mol``'s basis: its own if trained (6-31G,
+    6-31G**), else the 6-31G one (embedded in a 6-31G superset)."""
+    for gb in (B631GSS, B631G):
+        if os.path.exists(gb.weights):
+            try:
+                molecule_layout(mol, gb)
+            except ValueError:
+                continue
+            return DensityMLP.load(gb.weights)
+    return DensityMLP.load(WEIGHTS)
 
 
 def _embedded_prediction(net, mol):

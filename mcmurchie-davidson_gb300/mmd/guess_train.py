@@ -1,6 +1,7 @@
 """Train and evaluate the learned initial guess on seeded water clusters (6-31G).
 
     python -m mmd.guess_train --train 20000 --eval 500 --out DIR
+    python -m mmd.guess_train --basis 6-31gss --train 8000 --eval 64 --out DIR
 
 1. training data: converged RHF densities (direct, conver 1e-8) of seeded (H2O)n,
    n ~ U{1..6}, computed by the batched GPU path (1024 molecules per launch);
@@ -25,10 +26,10 @@ from .batch import BatchRHF
 from .clusters import water_cluster
 
 
-def converged_densities(geoms, chunk=1024, log=print):
+def converged_densities(geoms, basis="6-31g", chunk=1024, log=print):
     out = []
     for s in range(0, len(geoms), chunk):
-        br = BatchRHF(geoms[s:s + chunk], "6-31g")
+        br = BatchRHF(geoms[s:s + chunk], basis)
         br.run(conver=1e-8)
         Ph = br.P.cpu().numpy()
         out.extend(Ph[b, :n, :n].copy() for b, n in enumerate(br.N))
@@ -36,28 +37,28 @@ def converged_densities(geoms, chunk=1024, log=print):
     return out
 
 
-def dataset(mols, dens):
+def dataset(mols, dens, gb=G.B631G):
     F, Y, M = [], [], []
     for m, P in zip(mols, dens):
-        _, f, y, k, _ = G.molecule_samples(m, P)
+        _, f, y, k, _ = G.molecule_samples(m, P, gb)
         F.append(f)
         Y.append(y)
         M.append(k)
     return np.concatenate(F), np.concatenate(Y), np.concatenate(M)
 
 
-def evaluate(net, geoms, log=print):
+def evaluate(net, geoms, log=print, basis="6-31g"):
     """Core vs learned guess on the same molecules (batched, FP64, conver 1e-8): SCF
     iterations and wall time; then both again at conver 1e-10 with an FP64 polish
     build (BatchRHF.run(polish=True)) for the energy comparison."""
     from .molecule import Molecule
-    mols = [Molecule(g, "6-31g") for g in geoms]
+    mols = [Molecule(g, basis) for g in geoms]
     t0 = time.perf_counter()
     guesses = [G.predict_density(net, m) for m in mols]
     t_pred = time.perf_counter() - t0
     res = {}
     for name, gs in (("core", None), ("learned", guesses)):
-        br = BatchRHF(geoms, "6-31g")
+        br = BatchRHF(geoms, basis)
         t0 = time.perf_counter()
         br.run(conver=1e-8, guess=gs)
         t = time.perf_counter() - t0
@@ -93,11 +94,13 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--out", default="gpurun_out")
     ap.add_argument("--eval-only", action="store_true", help="evaluate the committed weights only")
+    ap.add_argument("--basis", default="6-31g", choices=sorted(G.BASES), help="basis of the network")
     args = ap.parse_args(argv)
+    gb = G.BASES[args.basis]
     from .molecule import Molecule
     eval_geoms = [water_cluster(8, seed=900000 + k) for k in range(args.eval)]
     if args.eval_only:
-        ev = evaluate(G.DensityMLP.load(), eval_geoms)
+        ev = evaluate(G.DensityMLP.load(gb.weights), eval_geoms, basis=args.basis)
         os.makedirs(args.out, exist_ok=True)
         with open(os.path.join(args.out, "guess_eval.json"), "w") as f:
             json.dump(ev, f, indent=1)
@@ -107,18 +110,18 @@ def main(argv=None):
     sizes = rng.integers(1, 7, size=args.train)
     train_geoms = [water_cluster(int(n), seed=200000 + k) for k, n in enumerate(sizes)]
     t0 = time.perf_counter()
-    dens = converged_densities(train_geoms)
+    dens = converged_densities(train_geoms, args.basis)
     t_data = time.perf_counter() - t0
-    mols = [Molecule(g, "6-31g") for g in train_geoms]
-    F, Y, M = dataset(mols, dens)
+    mols = [Molecule(g, args.basis) for g in train_geoms]
+    F, Y, M = dataset(mols, dens, gb)
     print(f"dataset: {len(F)} pair blocks from {len(mols)} clusters ({t_data:.1f} s of SCF)")
     t0 = time.perf_counter()
-    net = G.train(F, Y, M, epochs=args.epochs, log=print)
+    net = G.train(F, Y, M, epochs=args.epochs, log=print, gb=gb)
     t_train = time.perf_counter() - t0
     os.makedirs(args.out, exist_ok=True)
-    net.save(os.path.join(args.out, "guess_mlp_631g.npz"))
+    net.save(os.path.join(args.out, os.path.basename(gb.weights)))
     net.save()
-    ev = evaluate(net, eval_geoms)
+    ev = evaluate(net, eval_geoms, basis=args.basis)
     report = {"train_molecules": len(mols), "pair_blocks": int(len(F)), "data_scf_s": t_data, "train_s": t_train,
               "epochs": args.epochs, "loss_history": net.history, "evaluation": ev}
     with open(os.path.join(args.out, "guess_report.json"), "w") as f:

@@ -194,3 +194,31 @@ def test_embedding_places_631g_blocks_on_the_shared_functions():
     assert not P[rest].any() and not P[:, rest].any()
     with pytest.raises(ValueError):
         G.embed_density(small, Molecule(geom, "sto-3g"), Ps)
+
+
+def test_631gss_targets_are_rotation_invariant_with_d_functions():
+    """6-31G** layout (d sextet on O, p on H): a rotated molecule with the rotated
+    density (P_new = T(R^T)^T P T(R^T) per atom block) gives the same local-frame
+    targets, and assemble() inverts pair_targets()."""
+    from mmd import guess as G
+    from mmd.clusters import random_rotation
+    gb = G.B631GSS
+    m = _water_mol(2, seed=5)
+    from mmd.molecule import Molecule
+    m = Molecule(m.geometry_input, "6-31gss")
+    R = random_rotation(np.random.default_rng(3))
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((m.nbasis, m.nbasis))
+    P = A + A.T
+    Z, X, off = G.molecule_layout(m, gb)
+    T = np.zeros((m.nbasis, m.nbasis))
+    for a, z in enumerate(Z):
+        n = gb.nfunc[int(z)]
+        T[off[a]:off[a] + n, off[a]:off[a] + n] = G.block_transform(int(z), R.T, gb)
+    Prot = T.T @ P @ T
+    rot = Molecule(_rotated(m, R).geometry_input, "6-31gss")
+    pairs, _, Y1, _, (Zs, Rs, offs) = G.molecule_samples(m, P, gb)
+    _, _, Y2, _, _ = G.molecule_samples(rot, Prot, gb)
+    assert np.abs(Y1 - Y2).max() < 1e-4 * np.abs(Y1).max()
+    Pa = G.assemble(Y1, Zs, Rs, offs, pairs, m.nbasis, gb)
+    assert np.abs(Pa - P).max() < 1e-4 * np.abs(P).max()
