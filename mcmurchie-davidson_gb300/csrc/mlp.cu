@@ -14,6 +14,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/mmdg.h"
 #include "pairs.cuh"
 
@@ -38,20 +40,23 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* A, 
   __shared__ float Bs[TK][TN + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  // split K over blockIdx.z (the weight gradients: M x N small, K = batch rows)
+  const int kspan = (K + gridDim.z - 1) / gridDim.z;
+  const int kbeg = blockIdx.z * kspan, kend = min(K, kbeg + kspan);
   float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += TK) {
+  for (int k0 = kbeg; k0 < kend; k0 += TK) {
     for (int e = threadIdx.x; e < TK * TM; e += 256) {
       const int kk = e / TM, mm = e % TM;
       const int m = m0 + mm, k = k0 + kk;
       float v = 0.f;
-      if (m < M && k < K) v = ta ? ld(A, (long long)k * lda + m) : ld(A, (long long)m * lda + k);
+      if (m < M && k < kend) v = ta ? ld(A, (long long)k * lda + m) : ld(A, (long long)m * lda + k);
       As[kk][mm] = v;
     }
     for (int e = threadIdx.x; e < TK * TN; e += 256) {
       const int kk = e / TN, nn = e % TN;
       const int n = n0 + nn, k = k0 + kk;
       float v = 0.f;
-      if (n < N && k < K) v = tb ? ld(B, (long long)n * ldb + k) : ld(B, (long long)k * ldb + n);
+      if (n < N && k < kend) v = tb ? ld(B, (long long)n * ldb + k) : ld(B, (long long)k * ldb + n);
       Bs[kk][nn] = v;
     }
     __syncthreads();
@@ -76,7 +81,10 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const TA* A, 
       const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
       if (m < M && n < N) {
         float* c = C + (long long)m * ldc + n;
-        *c = beta != 0.f ? fmaf(beta, *c, acc[i][j]) : acc[i][j];
+        if (gridDim.z > 1)
+          atomicAdd(c, acc[i][j]);  // C zeroed by the launcher
+        else
+          *c = beta != 0.f ? fmaf(beta, *c, acc[i][j]) : acc[i][j];
       }
     }
 }
@@ -161,6 +169,17 @@ extern "C" int mmdg_mlp_gemm(int M, int N, int K, const void* A, int lda, int ta
   if (!M || !N) return MMDG_OK;
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   cudaStream_t st = (cudaStream_t)stream;
+  // few output tiles and a long K (weight gradients over a batch): split K over
+  // enough blocks to fill the GPU, partial tiles added with atomics into a zeroed C
+  const long long tiles = (long long)grid.x * grid.y;
+  if (beta == 0.f && tiles < 304 && K >= 1024) {
+    const int split = (int)std::min<long long>((K + 511) / 512, (608 + tiles - 1) / tiles);
+    if (split > 1) {
+      grid.z = split;
+      if (cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * ldc, st) != cudaSuccess)
+        return mmdg_internal_fail(MMDG_E_CUDA, "mmdg_mlp_gemm: memset");
+    }
+  }
   if (a_bf16 && !b_bf16)
     k_gemm<__nv_bfloat16, float><<<grid, 256, 0, st>>>(M, N, K, (const __nv_bfloat16*)A, lda, ta, (const float*)B, ldb,
                                                         tb, C, ldc, beta);

@@ -65,13 +65,13 @@ def test_rotated_targets_are_invariant():
 
 
 @pytest.mark.gpu
-def test_mlp_kernels_gradients_match_cpu_oracle():
+@pytest.mark.parametrize("B", [300, 5000])  # 5000 rows: the split-K weight-gradient GEMMs
+def test_mlp_kernels_gradients_match_cpu_oracle(B):
     import torch
     import mlp_oracle as O
     from mmd import guess as G
     net = G.DensityMLP(seed=3)
     rng = np.random.default_rng(9)
-    B = 300
     X = rng.standard_normal((B, G.NIN)).astype(np.float32)
     T = rng.standard_normal((B, G.NOUT)).astype(np.float32)
     M = (rng.random((B, G.NOUT)) < 0.6).astype(np.float32)
