@@ -52,6 +52,8 @@ FQ_PER_BUILD = 198282802.0
 # Fock build of this workload, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum; summary and command in profiles/k_fock_fp64_pipe_h2o16.md).
 DRAM_BYTES_PER_LAUNCH = {"1000": 47.7e6, "0000": 24.2e6, "1010": 25.5e6, "1110": 16.2e6, "2111": 5.3e6}
+# FP64-pipe busy fraction of the same launches (sm__pipe_fp64_cycles_active, same capture)
+FP64_PIPE_BUSY = {"1000": 0.730, "0000": 0.526, "1010": 0.688, "1110": 0.564, "2111": 0.682}
 
 
 def _env():
@@ -544,6 +546,7 @@ def gpu_arm(args):
     roofline = {"bound": "fp64", "kernel": "k_fock<MD_%d%d%d%d,double>" % dom_cls, "achieved": achieved,
                 "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": traffic,
                 "traffic_note": "DRAM bytes of one iteration-1 launch (ncu); the kernel is FP64-pipe bound",
+                "fp64_pipe_busy_ncu": FP64_PIPE_BUSY.get("%d%d%d%d" % dom_cls) if WORKLOAD["n_water"] == 16 else None,
                 "peak_source": "live DFMA probe mmdg_measure_peaks (MEASURED_PEAKS.json has no FP64 figure)",
                 "flops_per_launch": float(cls_flops[dom]) / builds, "launch_ms": float(class_ms[dom]) / builds,
                 "all_classes": {"achieved": all_achieved, "frac": all_achieved / fp64_peak,

@@ -222,3 +222,27 @@ def test_631gss_targets_are_rotation_invariant_with_d_functions():
     assert np.abs(Y1 - Y2).max() < 1e-4 * np.abs(Y1).max()
     Pa = G.assemble(Y1, Zs, Rs, offs, pairs, m.nbasis, gb)
     assert np.abs(Pa - P).max() < 1e-4 * np.abs(P).max()
+
+
+@pytest.mark.gpu
+def test_631gss_network_gains_over_core_guess():
+    """The committed 6-31G** network (mmd.guess_train --basis 6-31gss, 8000 clusters)
+    is the one network_for() picks for a 6-31G** molecule; on held-out (H2O)8 it cuts
+    the batched SCF iterations and the polished energies match the core-guess ones."""
+    from mmd import guess as G
+    from mmd.batch import BatchRHF
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    geoms = [water_cluster(8, seed=900000 + k) for k in range(4)]
+    net = G.network_for(Molecule(geoms[0], "6-31gss"))
+    assert net.gb is G.B631GSS
+    gs = [G.predict_density(net, Molecule(g, "6-31gss")) for g in geoms]
+    core = BatchRHF(geoms, "6-31gss")
+    core.run(conver=1e-8)
+    learned = BatchRHF(geoms, "6-31gss")
+    learned.run(conver=1e-8, guess=gs)
+    assert learned.converged.all() and not learned.reverted.any()
+    assert learned.iterations.mean() < 0.8 * core.iterations.mean()
+    Ec = core.run(conver=1e-10, polish=True)
+    El = learned.run(conver=1e-10, guess=gs, polish=True)
+    assert np.abs(El - Ec).max() < 1e-9
