@@ -126,8 +126,9 @@ class SCF(object):
         return float(torch.sum((Core + F) * P.T).item()) + self.nuc_energy
 
     # ---------------------------------------------------------------- pieces
-    def _two_electron(self, P, P_old):
-        """Unsymmetrised G(P - P_old) on the GPU, symmetrised: (G + G^T)/2."""
+    def _two_electron(self, P, P_old, symmetrize=True):
+        """G(P - P_old) on the GPU (formPT semantics), symmetrised (G + G^T)/2 unless
+        the caller does that itself (mmdg_fock_update)."""
         ctx = self.context
         t0 = time.perf_counter()
         dP = (P - P_old).contiguous().view(-1)
@@ -142,7 +143,7 @@ class SCF(object):
         self.fock_builds += 1
         self.fock_time += time.perf_counter() - t0
         G = G.view(self.nbasis, self.nbasis)
-        return 0.5 * (G + G.T)
+        return 0.5 * (G + G.T) if symmetrize else G
 
     def _conventional_fock(self, P):
         ctx = self.context
@@ -165,14 +166,19 @@ class SCF(object):
             del errorSet[0]
         n = len(fockSet)
         E = torch.stack(errorSet).reshape(n, -1)
-        B = torch.full((n + 1, n + 1), -1.0, dtype=torch.float64, device=F.device)
-        B[:n, :n] = E @ E.T
+        # the (n+1) x (n+1) DIIS system is solved on the host: one small copy back
+        # (which also yields ||error|| from the Gram diagonal) instead of a device
+        # solver call and a second synchronisation
+        gram = (E @ E.T).cpu().numpy()
+        B = -np.ones((n + 1, n + 1))
+        B[:n, :n] = gram
         B[n, n] = 0.0
-        rhs = torch.zeros(n + 1, dtype=torch.float64, device=F.device)
+        rhs = np.zeros(n + 1)
         rhs[n] = -1.0
-        w = torch.linalg.solve(B, rhs)
-        Fd = torch.einsum("i,ijk->jk", w[:n], torch.stack(fockSet))
-        return Fd, float(torch.linalg.norm(error).item())
+        w = np.linalg.solve(B, rhs)
+        wd = torch.as_tensor(w[:n], dtype=torch.float64, device=F.device)
+        Fd = torch.tensordot(wd, torch.stack(fockSet), dims=1)
+        return Fd, float(np.sqrt(max(gram[n - 1, n - 1], 0.0)))
 
     # ---------------------------------------------------------------- reference helpers
     def orthoFock(self):
@@ -281,9 +287,9 @@ class _RHFState:
             energy_old = self.energy
             if mol.direct:
                 self.last_dP = (self.P, self.P_old)
-                G = mol._two_electron(self.P, self.P_old)
+                G = mol._two_electron(self.P, self.P_old, symmetrize=False)
                 F = torch.empty_like(F_old)
-                mol.context.fock_update(G, F_old, F)
+                mol.context.fock_update(G, F_old, F)  # F = F_old + (G + G^T) / 2
                 self.F = F
             else:
                 self.F = mol._conventional_fock(self.P)
