@@ -279,16 +279,34 @@ __global__ void k_grad_one(GradArgs a) {
 }
 
 // ------------------------------------------------------------------ two-electron terms
-// One thread per unique shell quartet (bra pair ip >= ket pair iq); every unique
-// function quartet once, with the degeneracy of cython/fock.pyx:60-70 and the density
+// A warp per unique shell quartet (bra pair ip >= ket pair iq).  Every unique function
+// quartet counts once, with the degeneracy of cython/fock.pyx:60-70 and the density
 // factor 2 P_ij P_kl - (P_ik P_jl + P_il P_jk) / 2 (the exchange term averaged over the
-// quartet's permutations).
-__global__ void k_grad_two(GradArgs a) {
-  // a warp per shell quartet; its lanes split the bra component pairs
+// quartet's permutations); the warp keeps those weights in shared memory.  Per
+// primitive quartet the lanes share two transforms of the Hermite integrals R:
+//   W[cd][tuv]   = sum_{tau nu phi} E^cd (-1)^(tau+nu+phi) R[t+tau, u+nu, v+phi],
+//                  t+u+v up to the bra's L + 1 (one per ket component pair), and
+//   V[ab][tau..] = sum_{tuv} E^ab R[t+tau, u+nu, v+phi],
+//                  tau+nu+phi up to the ket's L + 1 (one per bra component pair);
+// the derivatives on the bra centres are then short sums of differentiated bra
+// coefficients against W, those on centre c of differentiated ket coefficients
+// against V, and centre d follows from translational invariance.
+constexpr int kGradWarps = 2;                          // warps per block
+constexpr int kHmax = (2 * kLmaxShell + 2) * (2 * kLmaxShell + 3) * (2 * kLmaxShell + 4) / 6;  // H(2l+1)
+constexpr int kNab = 36;                               // component pairs of a d-d pair
+constexpr int kGradSmemPerWarp = 2 * kNab * kHmax + kNab * kNab;  // W, V, weights (doubles)
+
+__device__ __forceinline__ int hcount(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
+
+__global__ void __launch_bounds__(32 * kGradWarps) k_grad_two(GradArgs a) {
+  extern __shared__ double gsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* Ws = gsm + warp * kGradSmemPerWarp;
+  double* Vs = Ws + kNab * kHmax;
+  double* Gam = Vs + kNab * kHmax;
   const long long q = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
   const long long nq = (long long)a.npair * (a.npair + 1) / 2;
-  if (q >= nq) return;
+  if (q >= nq) return;  // whole warps leave together (blockDim is a multiple of 32)
   // (ip, iq) from the triangular index q = ip (ip + 1) / 2 + iq
   int ip = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
   while ((long long)ip * (ip + 1) / 2 > q) --ip;
@@ -301,15 +319,52 @@ __global__ void k_grad_two(GradArgs a) {
     Ls[k] = a.L[s[k]];
     nc[k] = (Ls[k] + 1) * (Ls[k] + 2) / 2;
   }
+  const int nab = nc[0] * nc[1], ncd = nc[2] * nc[3];
+  const int Lp = Ls[0] + Ls[1], Lq = Ls[2] + Ls[3], M = Lp + Lq + 1;
+  const int HW = hcount(Lp + 1), HV = hcount(Lq + 1);
   const bool same_ab = s[0] == s[1], same_cd = s[2] == s[3], same_pair = ip == iq;
+  const int N = a.N;
+  // ---- density weights of the unique function quartets (0: not counted here)
+  for (int fq = lane; fq < nab * ncd; fq += 32) {
+    const int cab = fq / ncd, ccd = fq - cab * ncd;
+    const int ca = cab / nc[1], cb = cab - ca * nc[1], cc = ccd / nc[3], cd = ccd - cc * nc[3];
+    double w = 0.0;
+    int i = a.func[s[0] * kGradMaxComp + ca], j = a.func[s[1] * kGradMaxComp + cb];
+    int k = a.func[s[2] * kGradMaxComp + cc], l = a.func[s[3] * kGradMaxComp + cd];
+    const bool skip = (same_ab && ca < cb) || (same_cd && cc < cd) || (same_pair && cab < ccd) || i < 0 || j < 0 ||
+                      k < 0 || l < 0;
+    if (!skip) {
+      if (i < j) { int t = i; i = j; j = t; }
+      if (k < l) { int t = k; k = l; l = t; }
+      const int ij = i * (i + 1) / 2 + j, kl = k * (k + 1) / 2 + l;
+      if (ij < kl) {
+        int t = i; i = k; k = t;
+        t = j; j = l; l = t;
+      }
+      const double deg = (i != j ? 2.0 : 1.0) * (k != l ? 2.0 : 1.0) * (ij != kl ? 2.0 : 1.0);
+      const double* Pm = a.P;
+      const double gam = 2.0 * Pm[(long long)i * N + j] * Pm[(long long)k * N + l] -
+                         0.5 * (Pm[(long long)i * N + k] * Pm[(long long)j * N + l] +
+                                Pm[(long long)i * N + l] * Pm[(long long)j * N + k]);
+      int l3[4][3];
+      lmn_of(Ls[0], ca, l3[0][0], l3[0][1], l3[0][2]);
+      lmn_of(Ls[1], cb, l3[1][0], l3[1][1], l3[1][2]);
+      lmn_of(Ls[2], cc, l3[2][0], l3[2][1], l3[2][2]);
+      lmn_of(Ls[3], cd, l3[3][0], l3[3][1], l3[3][2]);
+      double nrm = 1.0;
+      for (int x = 0; x < 4; ++x)
+        for (int d = 0; d < 3; ++d) nrm *= comp_norm(l3[x][d]);
+      w = deg * gam * nrm;
+    }
+    Gam[fq] = w;
+  }
+  __syncwarp();
   double Cn[4][3];
   for (int k = 0; k < 4; ++k)
     for (int d = 0; d < 3; ++d) Cn[k][d] = a.center[3 * s[k] + d];
   double g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // centres a, b, c
   E1 Eb[3], Ek[3];
   double R[kRsize], F[kLtot + 2];
-  double W[6 * 6 * 6];
-  const int N = a.N;
   for (int k0 = 0; k0 < a.nprim[s[0]]; ++k0)
     for (int k1 = 0; k1 < a.nprim[s[1]]; ++k1) {
       const double ea = a.exps[a.poff[s[0]] + k0], eb = a.exps[a.poff[s[1]] + k1];
@@ -337,128 +392,115 @@ __global__ void k_grad_two(GradArgs a) {
                        (ec / qq) * (Cn[2][d] - Cn[3][d]));
           const double alpha = p * qq / (p + qq);
           const double X = P[0] - Q[0], Y = P[1] - Q[1], Z = P[2] - Q[2];
-          const int M = Ls[0] + Ls[1] + Ls[2] + Ls[3] + 1;
           boys_series(M, alpha * (X * X + Y * Y + Z * Z), F);
           hermite_r(M, alpha, X, Y, Z, F, R);
           const double pref = 2.0 * pow(kPi, 2.5) / (p * qq * sqrt(p + qq)) * Kab * Kcd;
-          for (int cab = lane; cab < nc[0] * nc[1]; cab += 32) {
-            {
-              const int ca = cab / nc[1], cb = cab - (cab / nc[1]) * nc[1];
-              if (same_ab && ca < cb) continue;
-              const int fi0 = a.func[s[0] * kGradMaxComp + ca], fj0 = a.func[s[1] * kGradMaxComp + cb];
-              if (fi0 < 0 || fj0 < 0) continue;
-              int la3[3], lb3[3];
-              lmn_of(Ls[0], ca, la3[0], la3[1], la3[2]);
-              lmn_of(Ls[1], cb, lb3[0], lb3[1], lb3[2]);
-              for (int cc = 0; cc < nc[2]; ++cc)
-                for (int cd = 0; cd < nc[3]; ++cd) {
-                  if (same_cd && cc < cd) continue;
-                  if (same_pair && (ca * nc[1] + cb) < (cc * nc[3] + cd)) continue;
-                  int i = fi0, j = fj0;
-                  int k = a.func[s[2] * kGradMaxComp + cc], l = a.func[s[3] * kGradMaxComp + cd];
-                  if (k < 0 || l < 0) continue;
-                  // canonical labels and degeneracy (cython/fock.pyx:24-70)
-                  if (i < j) { int t = i; i = j; j = t; }
-                  if (k < l) { int t = k; k = l; l = t; }
-                  const int ij = i * (i + 1) / 2 + j, kl = k * (k + 1) / 2 + l;
-                  if (ij < kl) {
-                    int t = i; i = k; k = t;
-                    t = j; j = l; l = t;
-                  }
-                  const double deg = (i != j ? 2.0 : 1.0) * (k != l ? 2.0 : 1.0) * (ij != kl ? 2.0 : 1.0);
-                  const double* Pm = a.P;
-                  const double gam = 2.0 * Pm[(long long)i * N + j] * Pm[(long long)k * N + l] -
-                                     0.5 * (Pm[(long long)i * N + k] * Pm[(long long)j * N + l] +
-                                            Pm[(long long)i * N + l] * Pm[(long long)j * N + k]);
-                  int lc3[3], ld3[3];
-                  lmn_of(Ls[2], cc, lc3[0], lc3[1], lc3[2]);
-                  lmn_of(Ls[3], cd, ld3[0], ld3[1], ld3[2]);
-                  const double nrm = comp_norm(la3[0]) * comp_norm(la3[1]) * comp_norm(la3[2]) *
-                                     comp_norm(lb3[0]) * comp_norm(lb3[1]) * comp_norm(lb3[2]) *
-                                     comp_norm(lc3[0]) * comp_norm(lc3[1]) * comp_norm(lc3[2]) *
-                                     comp_norm(ld3[0]) * comp_norm(ld3[1]) * comp_norm(ld3[2]);
-                  const double wgt = deg * gam * pref * nrm;
-                  if (wgt == 0.0) continue;
-                  // bra extents with one extra Hermite order for the bra derivatives
-                  const int bt = la3[0] + lb3[0] + 1, bu = la3[1] + lb3[1] + 1, bv = la3[2] + lb3[2] + 1;
-                  const int kt = lc3[0] + ld3[0], ku = lc3[1] + ld3[1], kv = lc3[2] + ld3[2];
-                  // ket-transformed R: W[t][u][v] = sum E^cd (-1)^(tau+nu+phi) R[t+tau][u+nu][v+phi]
-                  for (int t = 0; t <= bt; ++t)
-                    for (int u = 0; u <= bu; ++u)
-                      for (int v = 0; v <= bv; ++v) {
-                        double w = 0.0;
-                        for (int ta = 0; ta <= kt; ++ta)
-                          for (int nu = 0; nu <= ku; ++nu)
-                            for (int ph = 0; ph <= kv; ++ph) {
-                              const double e = Ek[0].v[lc3[0]][ld3[0]][ta] * Ek[1].v[lc3[1]][ld3[1]][nu] *
-                                               Ek[2].v[lc3[2]][ld3[2]][ph];
-                              w += ((ta + nu + ph) & 1 ? -e : e) * R[ridx(t + ta, u + nu, v + ph)];
-                            }
-                        W[(t * 6 + u) * 6 + v] = w;
-                      }
-                  // centres a and b
-                  for (int d = 0; d < 3; ++d) {
-                    double sa_ = 0.0, sb_ = 0.0;
-                    for (int t = 0; t <= bt; ++t)
-                      for (int u = 0; u <= bu; ++u)
-                        for (int v = 0; v <= bv; ++v) {
-                          const int tt[3] = {t, u, v};
-                          double ea_ = 1.0, eb_ = 1.0;
-                          for (int e = 0; e < 3; ++e) {
-                            const double base = Eb[e].v[la3[e]][lb3[e]][tt[e]];
-                            if (e == d) {
-                              double da = 2.0 * ea * Eb[e].v[la3[e] + 1][lb3[e]][tt[e]];
-                              if (la3[e] > 0) da -= la3[e] * Eb[e].v[la3[e] - 1][lb3[e]][tt[e]];
-                              double db = 2.0 * eb * Eb[e].v[la3[e]][lb3[e] + 1][tt[e]];
-                              if (lb3[e] > 0) db -= lb3[e] * Eb[e].v[la3[e]][lb3[e] - 1][tt[e]];
-                              ea_ *= da;
-                              eb_ *= db;
-                            } else {
-                              ea_ *= base;
-                              eb_ *= base;
-                            }
-                          }
-                          const double w = W[(t * 6 + u) * 6 + v];
-                          sa_ += ea_ * w;
-                          sb_ += eb_ * w;
-                        }
-                    g[0][d] += wgt * sa_;
-                    g[1][d] += wgt * sb_;
-                  }
-                  // centre c: ket derivative coefficients, bra without the extra order
-                  for (int d = 0; d < 3; ++d) {
-                    double sc_ = 0.0;
-                    const int kte[3] = {kt + (d == 0), ku + (d == 1), kv + (d == 2)};
-                    for (int t = 0; t <= bt - 1; ++t)
-                      for (int u = 0; u <= bu - 1; ++u)
-                        for (int v = 0; v <= bv - 1; ++v) {
-                          const double eab = Eb[0].v[la3[0]][lb3[0]][t] * Eb[1].v[la3[1]][lb3[1]][u] *
-                                             Eb[2].v[la3[2]][lb3[2]][v];
-                          if (eab == 0.0) continue;
-                          double w = 0.0;
-                          for (int ta = 0; ta <= kte[0]; ++ta)
-                            for (int nu = 0; nu <= kte[1]; ++nu)
-                              for (int ph = 0; ph <= kte[2]; ++ph) {
-                                const int tk[3] = {ta, nu, ph};
-                                double e = 1.0;
-                                for (int x = 0; x < 3; ++x) {
-                                  if (x == d) {
-                                    double dc = 2.0 * ec * Ek[x].v[lc3[x] + 1][ld3[x]][tk[x]];
-                                    if (lc3[x] > 0) dc -= lc3[x] * Ek[x].v[lc3[x] - 1][ld3[x]][tk[x]];
-                                    e *= dc;
-                                  } else {
-                                    e *= Ek[x].v[lc3[x]][ld3[x]][tk[x]];
-                                  }
-                                }
-                                w += ((ta + nu + ph) & 1 ? -e : e) * R[ridx(t + ta, u + nu, v + ph)];
-                              }
-                          sc_ += eab * w;
-                        }
-                    g[2][d] += wgt * sc_;
-                  }
+          // ---- W: one ket component pair per lane
+          for (int ccd = lane; ccd < ncd; ccd += 32) {
+            const int cc = ccd / nc[3], cd = ccd - cc * nc[3];
+            int lc3[3], ld3[3];
+            lmn_of(Ls[2], cc, lc3[0], lc3[1], lc3[2]);
+            lmn_of(Ls[3], cd, ld3[0], ld3[1], ld3[2]);
+            double* W = Ws + ccd * HW;
+            for (int h = 0; h < HW; ++h) W[h] = 0.0;
+            for (int ta = 0; ta <= lc3[0] + ld3[0]; ++ta)
+              for (int nu = 0; nu <= lc3[1] + ld3[1]; ++nu)
+                for (int ph = 0; ph <= lc3[2] + ld3[2]; ++ph) {
+                  double e = Ek[0].v[lc3[0]][ld3[0]][ta] * Ek[1].v[lc3[1]][ld3[1]][nu] * Ek[2].v[lc3[2]][ld3[2]][ph];
+                  if (e == 0.0) continue;
+                  if ((ta + nu + ph) & 1) e = -e;
+                  for (int t = 0; t <= Lp + 1; ++t)
+                    for (int u = 0; u <= Lp + 1 - t; ++u)
+                      for (int v = 0; v <= Lp + 1 - t - u; ++v)
+                        W[ridx(t, u, v)] += e * R[ridx(t + ta, u + nu, v + ph)];
                 }
+          }
+          // ---- V: one bra component pair per lane
+          for (int cab = lane; cab < nab; cab += 32) {
+            const int ca = cab / nc[1], cb = cab - ca * nc[1];
+            int la3[3], lb3[3];
+            lmn_of(Ls[0], ca, la3[0], la3[1], la3[2]);
+            lmn_of(Ls[1], cb, lb3[0], lb3[1], lb3[2]);
+            double* V = Vs + cab * HV;
+            for (int h = 0; h < HV; ++h) V[h] = 0.0;
+            for (int t = 0; t <= la3[0] + lb3[0]; ++t)
+              for (int u = 0; u <= la3[1] + lb3[1]; ++u)
+                for (int v = 0; v <= la3[2] + lb3[2]; ++v) {
+                  const double e = Eb[0].v[la3[0]][lb3[0]][t] * Eb[1].v[la3[1]][lb3[1]][u] * Eb[2].v[la3[2]][lb3[2]][v];
+                  if (e == 0.0) continue;
+                  for (int ta = 0; ta <= Lq + 1; ++ta)
+                    for (int nu = 0; nu <= Lq + 1 - ta; ++nu)
+                      for (int ph = 0; ph <= Lq + 1 - ta - nu; ++ph)
+                        V[ridx(ta, nu, ph)] += e * R[ridx(t + ta, u + nu, v + ph)];
+                }
+          }
+          __syncwarp();
+          // ---- derivatives of every function quartet
+          for (int fq = lane; fq < nab * ncd; fq += 32) {
+            const double wgt = Gam[fq];
+            if (wgt == 0.0) continue;
+            const int cab = fq / ncd, ccd = fq - cab * ncd;
+            const int ca = cab / nc[1], cb = cab - ca * nc[1], cc = ccd / nc[3], cd = ccd - cc * nc[3];
+            int la3[3], lb3[3], lc3[3], ld3[3];
+            lmn_of(Ls[0], ca, la3[0], la3[1], la3[2]);
+            lmn_of(Ls[1], cb, lb3[0], lb3[1], lb3[2]);
+            lmn_of(Ls[2], cc, lc3[0], lc3[1], lc3[2]);
+            lmn_of(Ls[3], cd, ld3[0], ld3[1], ld3[2]);
+            const double* W = Ws + ccd * HW;
+            const double* V = Vs + cab * HV;
+            const double w = wgt * pref;
+            for (int d = 0; d < 3; ++d) {
+              // centres a and b against W (bra extent one higher along d)
+              double sa_ = 0.0, sb_ = 0.0;
+              const int ext[3] = {la3[0] + lb3[0] + (d == 0), la3[1] + lb3[1] + (d == 1), la3[2] + lb3[2] + (d == 2)};
+              for (int t = 0; t <= ext[0]; ++t)
+                for (int u = 0; u <= ext[1]; ++u)
+                  for (int v = 0; v <= ext[2]; ++v) {
+                    const int tt[3] = {t, u, v};
+                    double ea_ = 1.0, eb_ = 1.0;
+                    for (int e = 0; e < 3; ++e) {
+                      if (e == d) {
+                        double da = 2.0 * ea * Eb[e].v[la3[e] + 1][lb3[e]][tt[e]];
+                        if (la3[e] > 0) da -= la3[e] * Eb[e].v[la3[e] - 1][lb3[e]][tt[e]];
+                        double db = 2.0 * eb * Eb[e].v[la3[e]][lb3[e] + 1][tt[e]];
+                        if (lb3[e] > 0) db -= lb3[e] * Eb[e].v[la3[e]][lb3[e] - 1][tt[e]];
+                        ea_ *= da;
+                        eb_ *= db;
+                      } else {
+                        const double base = Eb[e].v[la3[e]][lb3[e]][tt[e]];
+                        ea_ *= base;
+                        eb_ *= base;
+                      }
+                    }
+                    const double wv = W[ridx(t, u, v)];
+                    sa_ += ea_ * wv;
+                    sb_ += eb_ * wv;
+                  }
+              // centre c against V (ket extent one higher along d)
+              double sc_ = 0.0;
+              const int kex[3] = {lc3[0] + ld3[0] + (d == 0), lc3[1] + ld3[1] + (d == 1), lc3[2] + ld3[2] + (d == 2)};
+              for (int ta = 0; ta <= kex[0]; ++ta)
+                for (int nu = 0; nu <= kex[1]; ++nu)
+                  for (int ph = 0; ph <= kex[2]; ++ph) {
+                    const int tk[3] = {ta, nu, ph};
+                    double e = 1.0;
+                    for (int x = 0; x < 3; ++x) {
+                      if (x == d) {
+                        double dc = 2.0 * ec * Ek[x].v[lc3[x] + 1][ld3[x]][tk[x]];
+                        if (lc3[x] > 0) dc -= lc3[x] * Ek[x].v[lc3[x] - 1][ld3[x]][tk[x]];
+                        e *= dc;
+                      } else {
+                        e *= Ek[x].v[lc3[x]][ld3[x]][tk[x]];
+                      }
+                    }
+                    sc_ += ((ta + nu + ph) & 1 ? -e : e) * V[ridx(ta, nu, ph)];
+                  }
+              g[0][d] += w * sa_;
+              g[1][d] += w * sb_;
+              g[2][d] += w * sc_;
             }
           }
+          __syncwarp();
         }
     }
   for (int x = 0; x < 3; ++x)
@@ -483,6 +525,10 @@ cudaError_t mmdg_launch_rhf_gradient(const GradArgs& a, cudaStream_t st) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const long long nq = (long long)a.npair * (a.npair + 1) / 2;
-  k_grad_two<<<(unsigned)((nq * 32 + 127) / 128), 128, 0, st>>>(a);
+  const size_t smem = sizeof(double) * kGradSmemPerWarp * kGradWarps;
+  e = cudaFuncSetAttribute(k_grad_two, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long nthreads = nq * 32;
+  k_grad_two<<<(unsigned)((nthreads + 32 * kGradWarps - 1) / (32 * kGradWarps)), 32 * kGradWarps, smem, st>>>(a);
   return cudaGetLastError();
 }
