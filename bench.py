@@ -60,6 +60,24 @@ def _env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+# ------------------------------------------------------------------------------ ranks
+def max_over_ranks(t_local: float, device: str = "cpu") -> float:
+    """The slowest rank's time (all-reduce MAX); the local time without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(t_local)
+    t = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, units_per_rank: int, t_max: float) -> float:
+    """Whole-job throughput of independent replicas: all ranks' units over the slowest
+    rank's time (weak scaling: every rank runs the full workload)."""
+    return world * units_per_rank / t_max
+
+
 # ------------------------------------------------------------------------------ clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -521,12 +539,9 @@ def gpu_arm(args):
     prof = mol._fock_profile
     mol._fock_profile = None
     t_dev = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(t_dev, "cuda")
     builds = args.steps
-    value = world * builds / t_dev
+    value = replica_throughput(world, builds, t_dev)
     counts = prof["counts"].reshape(-1, 3)
     class_ms = prof["class_ms"]
     fq_per_build = float(counts[:, 0].sum()) / builds
