@@ -608,9 +608,9 @@ def gpu_arm(args):
                    "quartets_per_s_1core": cb["quartets_per_s_1core"]}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "error": str(e)[:300]}
-    # our kernels per Fock build: |dP| copy, shell-block maxima, one launch per class
-    # (two with the FP32 split), symmetrised update
-    launches_per_build = 3 + len(flop_model.CLASSES) * (2 if fp32 > 0 else 1)
+    # our kernels per Fock build: k_prep_density, k_shell_dmax, one k_screen per class,
+    # one k_fock per class and precision, and k_fock_update of the SCF step
+    launches_per_build = 3 + len(flop_model.CLASSES) * (3 if fp32 > 0 else 2)
     batched = mixed = combined = None
     if rank == 0 and not args.no_batch:
         try:

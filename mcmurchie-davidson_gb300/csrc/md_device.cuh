@@ -70,9 +70,12 @@ struct Geometry {
 template <int L>
 __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double T, double* Fn) {
   if (T < kBoysTaylorMax) {
-    int k = __double2int_rn(T * 16.0);
-    k = min(max(k, 0), kBoysNGrid - 1);
-    const double y = fma(double(k), 0.0625, -T);  // T_k - T
+    // k = round(16 T) without FP64<->int conversions (which issue on the FP64 pipe):
+    // adding 1.5 * 2^52 leaves round(16 T) in the low mantissa bits (0 <= 16 T < 767.5)
+    constexpr double kRound = 6755399441055744.0;
+    const double r = fma(T, 16.0, kRound);
+    const int k = __double2loint(r);
+    const double y = fma(r - kRound, 0.0625, -T);  // T_k - T
     const double* __restrict__ c = tab + (L * kBoysNGrid + k) * kBoysRow;
     double f = fma(c[6], y, c[5]);
     f = fma(f, y, c[4]);
