@@ -45,7 +45,7 @@ def nnz(la: int, lb: int) -> int:
 
 
 def prim_quartet_flops(la, lb, lc, ld) -> int:
-    """Survey model: FLOPs per primitive quartet (dense transforms)."""
+    """Model FLOPs per primitive quartet (dense Hermite transforms)."""
     Lp, Lq = la + lb, lc + ld
     L = Lp + Lq
     f_boys = 2 * (L + 1) + 10

@@ -92,7 +92,7 @@ def main(argv=None):
     ap.add_argument("--train", type=int, default=20000)
     ap.add_argument("--eval", type=int, default=500)
     ap.add_argument("--epochs", type=int, default=30)
-    ap.add_argument("--out", default="gpurun_out")
+    ap.add_argument("--out", default="guess_out")
     ap.add_argument("--eval-only", action="store_true", help="evaluate the committed weights only")
     ap.add_argument("--basis", default="6-31g", choices=sorted(G.BASES), help="basis of the network")
     args = ap.parse_args(argv)

@@ -34,7 +34,7 @@ HOST_EIGH_MAX_N = 1024
 
 def host_eigh(A):
     """One symmetric eigensolve on the host cores: LAPACK dsyevd through SciPy (on the
-    Grace host 0.64 ms at N = 104 against 2.8 ms for numpy.linalg.eigh; 7.4 ms at
+    16-core Grace CPU 0.64 ms at N = 104 against 2.8 ms for numpy.linalg.eigh; 7.4 ms at
     N = 400 and 28 ms at N = 800, where cuSOLVER's syevd takes 11.8 and 31 ms).  Many
     small solves at once (the batched SCF) stay on numpy.linalg.eigh in a thread pool:
     SciPy's wrapper serialises there (1.14 s against 0.45 s for 1024 matrices)."""

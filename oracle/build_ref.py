@@ -3,7 +3,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product package imports this file or
 anything it builds; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs
-of ``bench.py`` use ``oracle/``, and only as the checker / the timed CPU baseline.
+of ``bench.py`` use ``oracle/``, and only to check results or as the timed CPU baseline.
 
 What it does
 ------------
@@ -21,7 +21,7 @@ current toolchain needs (applied to a temporary copy, never to the original):
    normalisation (``basis.pxi:102-110``) would divide by zero.  The shim binds
    ``fact2 = factorial2(n, extend="complex")`` which gives 1, 1, 3 at -1, 1, 3.
 
-Outputs go only under ``oracle/_ref/`` (git-ignored, but shipped to the GPU host):
+Outputs go only under ``oracle/_ref/`` (git-ignored, but copied with the tree to the machine with the GPU):
 
 * ``oracle/_ref/gen/*.c``          Cython-generated C (portable; rebuilt per host)
 * ``oracle/_ref/mmd/integrals/*.so`` the compiled modules, importable as
@@ -34,7 +34,7 @@ Modes
 ``python oracle/build_ref.py``            cythonize from the reference (needs the
                                            reference tree and Cython) and compile.
 ``python oracle/build_ref.py --compile``  compile the already-generated C (the
-                                           GPU host has neither the reference nor
+                                           GPU machine has neither the reference nor
                                            Cython; it only needs gcc, Python.h and
                                            NumPy's headers).
 ``python oracle/build_ref.py --full DIR`` additionally lay out a complete shimmed

@@ -2,7 +2,7 @@
  * mmd_oracle.c -- CPU restatement of the reference's two-electron hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is the oracle: the parity tests, smoke() and
- * the CPU-baseline leg of bench.py call it as the checker.  The product library
+ * the CPU-baseline leg of bench.py call it to check results.  The product library
  * (libmmdg.so) never links, loads or calls it.
  *
  * Every function restates one routine of jjgoings/McMurchie-Davidson, cited by
@@ -10,8 +10,8 @@
  * (same recursions, same loop order, same screening and degeneracy rules) so
  * that results agree to rounding.  The only piece that is not a restatement of
  * reference code is the Boys function: the reference calls SciPy's
- * ``scipy.special.cython_special.hyp1f1`` (third-party; SciPy 1.18.1 in the
- * build container, unpinned by the reference's requirements.txt:2 "scipy>=0.19.0"),
+ * ``scipy.special.cython_special.hyp1f1`` (third-party; SciPy 1.18.1 where the
+ * fixtures were made, unpinned by the reference's requirements.txt:2 "scipy>=0.19.0"),
  * evaluating F_m(T) = 1F1(m+1/2; m+3/2; -T) / (2m+1)   (cython/util.pxi:54-55).
  * Here 1F1 is evaluated through Kummer's transformation
  *     1F1(a; b; -T) = exp(-T) 1F1(b-a; b; T),  b-a = 1,

@@ -1,6 +1,6 @@
 """Python face of the oracle (TEST INFRASTRUCTURE ONLY).
 
-The oracle is the checker for the GPU path: ``tests/``, ``__graft_entry__.smoke()``
+The oracle checks the GPU path: ``tests/``, ``__graft_entry__.smoke()``
 and ``bench.py``'s CPU-baseline leg may import it; the product package never does.
 
 Two backends live here, both restating / running the reference's hot path:

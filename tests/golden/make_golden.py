@@ -22,7 +22,7 @@ the reference's own outputs:
                           or two recorded ``formPT`` calls (inputs and output).
 
 The fixtures are committed; this script is committed beside them so they can be
-regenerated.  Nothing on the GPU host runs it.
+regenerated.  Nothing on the GPU machine runs it.
 """
 from __future__ import annotations
 

@@ -4,7 +4,7 @@
   (its own places=12 check plus relative 1e-9; the literature values are only
   good to ~7e-10 relative) and an mpmath grid (relative 5e-15);
 * contracted ERIs of every angular class, the full water/STO-3G tensor and the
-  Schwarz tables: the compiled reference run in the build container;
+  Schwarz tables: the compiled reference, run to make the fixtures;
 * formPT: the reference's own recorded calls (inputs and unsymmetrised output).
 """
 import json
