@@ -143,9 +143,11 @@ int mmdg_set_prim_tol(mmdg_context* ctx, double tol);
  * energy-weighted density (device, N x N, the reference's P = C_occ C_occ^T);
  * atom_xyz (bohr, natom x 3), atom_Z and shell_atom (the atom of every shell of the
  * basis) are host arrays; grad (host, natom x 3) receives dE/dR including the nuclear
- * repulsion (the reference's forces are -grad).  One molecule per context. */
+ * repulsion (the reference's forces are -grad).  Shell quartets with Schwarz bounds
+ * Q_ab Q_cd < qtol are skipped (0: none; the reference skips none).  One molecule per
+ * context. */
 int mmdg_rhf_gradient(mmdg_context* ctx, const double* P, const double* W, int natom, const double* atom_xyz,
-                      const double* atom_Z, const int* shell_atom, double* grad, void* stream);
+                      const double* atom_Z, const int* shell_atom, double qtol, double* grad, void* stream);
 
 /* mmdg_fock replayed as one CUDA graph: the first call with a given (dP, G, tol,
  * fp32_below) runs the build eagerly and captures its launches (screening, class

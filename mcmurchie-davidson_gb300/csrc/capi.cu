@@ -1508,8 +1508,8 @@ extern "C" int mmdg_set_tuning(mmdg_context* h, int cls, int grid_blocks) {
 #include "grad.cuh"
 
 extern "C" int mmdg_rhf_gradient(mmdg_context* h, const double* P, const double* W, int natom,
-                                 const double* atom_xyz, const double* atom_Z, const int* shell_atom, double* grad,
-                                 void* stream) {
+                                 const double* atom_xyz, const double* atom_Z, const int* shell_atom, double qtol,
+                                 double* grad, void* stream) {
   if (!h || !P || !W || !atom_xyz || !atom_Z || !shell_atom || !grad || natom < 1)
     return fail(MMDG_E_ARG, "mmdg_rhf_gradient: null argument");
   if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_rhf_gradient: no basis set");
@@ -1538,8 +1538,9 @@ extern "C" int mmdg_rhf_gradient(mmdg_context* h, const double* P, const double*
   a.center = h->d_center.p;
   a.exps = h->d_exp.p;
   a.coefs = h->d_coef.p;
-  a.Qpair = nullptr;
-  a.qtol = 0.0;
+  if (!(qtol >= 0.0)) return fail(MMDG_E_ARG, "mmdg_rhf_gradient: qtol must be >= 0");
+  a.Qpair = qtol > 0.0 ? h->d_Q.p : nullptr;
+  a.qtol = qtol;
   a.natom = natom;
   a.xyz = dxyz.p;
   a.Z = dZ.p;

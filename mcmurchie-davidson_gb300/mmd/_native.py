@@ -46,7 +46,7 @@ def _bind(L):
         "mmdg_set_tuning": (c_int, [p, c_int, c_int]),
         "mmdg_set_streams": (c_int, [p, c_int]),
         "mmdg_set_prim_tol": (c_int, [p, ctypes.c_double]),
-        "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, p, p]),
+        "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, c_d, p, p]),
         "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),
     }
     for name, (res, args) in sig.items():

@@ -18,11 +18,18 @@ import numpy as np
 from . import _native
 
 
+# Schwarz screening of the two-electron derivative terms: a derivative integral is at
+# most ~2 sqrt(exponent) times the integral bound Q_ab Q_cd, and the density factor at
+# most a few units, so skipped quartets change a force by < 1e-12 each at 1e-16
+GRADIENT_SCHWARZ_TOL = 1e-16
+
+
 class Forces:
     """Nuclear gradient methods for the molecule object (mmd/forces.py:6-97)."""
 
-    def forces(self):
-        """Compute the nuclear forces of the converged RHF state."""
+    def forces(self, qtol=GRADIENT_SCHWARZ_TOL):
+        """Compute the nuclear forces of the converged RHF state.  ``qtol``: shell
+        quartets with Q_ab Q_cd below it are skipped (0 keeps all, as the reference)."""
         if not self.is_converged:
             sys.exit("Need to converge SCF before computing gradient")
         ctx = self.context
@@ -43,7 +50,8 @@ class Forces:
         lib = _native.lib()
         _native.check(lib.mmdg_rhf_gradient(ctx._h, ctypes.c_void_p(Pd.data_ptr()), ctypes.c_void_p(Wd.data_ptr()),
                                             natom, _native._ptr(xyz), _native._ptr(Z), _native._ptr(shell_atom),
-                                            _native._ptr(grad), _native.stream_ptr()), "mmdg_rhf_gradient")
+                                            float(qtol), _native._ptr(grad), _native.stream_ptr()),
+                      "mmdg_rhf_gradient")
         grad = grad.reshape(natom, 3)
         for a, atom in enumerate(self.atoms):
             atom.forces = -grad[a]

@@ -71,3 +71,15 @@ def test_cluster_forces_have_no_net_force_or_torque(built_lib):
     R = np.array([a.origin for a in mol.atoms])
     assert np.abs(f.sum(axis=0)).max() < 1e-10
     assert np.abs(np.cross(R, f).sum(axis=0)).max() < 1e-7
+
+
+def test_schwarz_screened_forces_equal_unscreened(built_lib):
+    """Skipping shell quartets with Q_ab Q_cd < 1e-16 (the default) changes no force
+    component by more than 1e-11 on a spread-out (H2O)6 cluster."""
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    mol = Molecule(water_cluster(6, seed=8), "6-31g")
+    mol.RHF(doPrint=False, conver=1e-10)
+    f_all = mol.forces(qtol=0.0).copy()
+    f_scr = mol.forces()
+    assert np.abs(f_scr - f_all).max() < 1e-11
