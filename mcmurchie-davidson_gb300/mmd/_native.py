@@ -15,6 +15,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmmdg.so")
 NCLASS = 21
+DEFAULT_STREAMS_SINGLE = 4
 MAX_COMP = 6
 LMAX = 2
 
@@ -122,6 +123,11 @@ class Context:
         with torch.cuda.device(self.device):
             check(lib().mmdg_set_basis(h, self.nmol, _ptr(self.nfunc), self.nshell, _ptr(mol), _ptr(L), _ptr(K),
                                        _ptr(cen), _ptr(ex), _ptr(co), _ptr(fn)), "mmdg_set_basis")
+        if self.nmol == 1:
+            # one molecule: the class kernels of a Fock build run on four concurrent
+            # streams (the autotuner's choice on (H2O)16 / 6-31G**: 52.7 against 62.1 ms
+            # per build in FP64, 31.4 against 43.5 ms mixed); batched contexts keep one
+            check(lib().mmdg_set_streams(h, DEFAULT_STREAMS_SINGLE), "mmdg_set_streams")
         self.nn = int(np.sum(self.nfunc.astype(np.int64) ** 2))
         self.ntri = int(np.sum(self.nfunc.astype(np.int64) * (self.nfunc + 1) // 2))
         self.base = np.concatenate([[0], np.cumsum(self.nfunc.astype(np.int64) ** 2)[:-1]])
