@@ -124,8 +124,8 @@ long long mmdg_boys_table(double* out, long long n);
 /* Autotuner hooks (no counterpart in the reference).  mmdg_set_tuning sets the
  * persistent grid of angular class `cls` (0..MMDG_NCLASS-1, the order of the class
  * table: (ss|ss), (ps|ss), (ps|ps), (pp|ss), ...; 0 = one full wave at the kernel's
- * occupancy); mmdg_set_streams spreads the class kernels over 1..4 concurrent
- * streams (fork/join on events). */
+ * occupancy); mmdg_set_streams spreads the classes (screening and evaluation) over
+ * 1..8 concurrent streams (fork/join on events). */
 int mmdg_set_tuning(mmdg_context* ctx, int cls, int grid_blocks);
 int mmdg_set_streams(mmdg_context* ctx, int nstreams);
 

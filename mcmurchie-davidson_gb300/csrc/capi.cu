@@ -186,6 +186,7 @@ static int nnz_pair(int la, int lb) {
 }
 static int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
 static const int kNumPairClasses = (MMDG_LMAX + 1) * (MMDG_LMAX + 2) / 2;
+static const int kMaxStreams = 8;  // concurrent class streams of a Fock build
 
 struct mmdg_context {
   int device = 0;
@@ -226,8 +227,8 @@ struct mmdg_context {
   // tuning (autotuner): persistent grid per class (0 = occupancy), concurrent class streams
   int class_grid[MMDG_NCLASS] = {0};
   int nstreams = 1;
-  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t fork_ev = nullptr, join_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t side[kMaxStreams] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kMaxStreams] = {};
   // CUDA graph of one Fock build (mmdg_fock_graph)
   cudaGraphExec_t graph = nullptr;
   const double* g_dP = nullptr;
@@ -318,7 +319,7 @@ extern "C" int mmdg_destroy(mmdg_context* h) {
   if (!h) return MMDG_OK;
   DeviceGuard dg(h->device);
   if (h->graph) cudaGraphExecDestroy(h->graph);
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < kMaxStreams; ++k) {
     if (h->side[k]) cudaStreamDestroy(h->side[k]);
     if (h->join_ev[k]) cudaEventDestroy(h->join_ev[k]);
   }
@@ -973,7 +974,13 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   cudaEvent_t ev[2 * MMDG_NCLASS];
   if (class_ms)
     for (int k = 0; k < 2 * MMDG_NCLASS; ++k) CUDA_TRY(cudaEventCreate(&ev[k]));
-  // ---- screening passes (all classes), then evaluation
+  // ---- screening and evaluation of every class; with several streams class c runs
+  // both on stream c mod n (fork / join on events), so classes overlap
+  const int ns = class_ms ? 1 : h->nstreams;
+  if (ns > 1) {
+    CUDA_TRY(cudaEventRecord(h->fork_ev, st));
+    for (int k = 0; k < ns; ++k) CUDA_TRY(cudaStreamWaitEvent(h->side[k], h->fork_ev, 0));
+  }
   int ci = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
@@ -989,23 +996,16 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
                       h->d_gslot[ck].p,
                       h->ngroup[ck],
                       h->nkeys[ci]};
-      k_screen<<<cl.nbra, kThreads, 0, st>>>(g, f, cl, ql);
+      k_screen<<<cl.nbra, kThreads, 0, ns > 1 ? h->side[ci % ns] : st>>>(g, f, cl, ql);
       CUDA_TRY(cudaGetLastError());
     }
     ++ci;
   }
-  // class kernels, optionally spread over concurrent streams (fork / join on events)
-  const int ns = class_ms ? 1 : h->nstreams;
-  if (ns > 1) {
-    CUDA_TRY(cudaEventRecord(h->fork_ev, st));
-    for (int k = 0; k < ns; ++k) CUDA_TRY(cudaStreamWaitEvent(h->side[k], h->fork_ev, 0));
-  }
   ci = 0;
-  int launched = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
     f.counters = h->d_counters.p + 3 * ci;
-    cudaStream_t cs = ns > 1 ? h->side[launched % ns] : st;
+    cudaStream_t cs = ns > 1 ? h->side[ci % ns] : st;
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
     if (h->cls_count[cb] && h->cls_count[ck]) {
       ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split,
@@ -1016,7 +1016,6 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
       if (split > 0.f)
         CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + h->total_keys + h->kbase[ci], ko,
                         h->nkeys[ci], grid, cs));
-      ++launched;
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;
@@ -1578,7 +1577,7 @@ extern "C" int mmdg_set_prim_tol(mmdg_context* h, double tol) {
 
 extern "C" int mmdg_set_streams(mmdg_context* h, int nstreams) {
   if (!h) return fail(MMDG_E_ARG, "mmdg_set_streams: null context");
-  if (nstreams < 1 || nstreams > 4) return fail(MMDG_E_ARG, "mmdg_set_streams: 1 to 4 streams");
+  if (nstreams < 1 || nstreams > kMaxStreams) return fail(MMDG_E_ARG, "mmdg_set_streams: 1 to 8 streams");
   DeviceGuard dg(h->device);
   if (!h->fork_ev) CUDA_TRY(cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
   for (int k = 0; k < nstreams; ++k) {

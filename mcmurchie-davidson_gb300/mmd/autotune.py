@@ -5,11 +5,13 @@ Tunables (C ABI ``mmdg_set_tuning`` / ``mmdg_set_streams``):
 * per angular class, the persistent grid of its evaluation kernel: one full wave at
   the kernel's occupancy (0), or k blocks per SM for k in {1, 2, 4} -- small grids
   pack the tail of small classes, full waves hide latency in large ones;
-* the number of concurrent streams the 21 class kernels are spread over (1, 2, 4):
-  small batches leave the GPU half empty with one class at a time.
+* the number of concurrent streams the 21 classes (screening and evaluation) are
+  spread over (1, 2, 4, 8): one class at a time leaves the GPU idle in the small
+  classes and in every kernel's tail;
+* with several streams, one grid size for all classes, timed as whole builds.
 
 Each candidate is timed with CUDA events on a representative density difference
-(``mmdg_fock_timed`` per class for the grids, whole builds for the streams).
+(``mmdg_fock_timed`` per class for the per-class grids, whole builds otherwise).
 Results are cached as JSON under ``_build/tuning.json`` keyed by the GPU name and
 the basis signature (molecules, functions, shells).
 """
@@ -93,13 +95,24 @@ def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuni
                 grids[c] = g
     stream_ms = {}
     best_s, best_t = 1, np.inf
-    for s in (1, 2, 4):
+    for s in (1, 2, 4, 8):
         Tuning(grids, s).apply(ctx)
         t = _time_build(ctx, dP, tol, fp32_below, reps)
         stream_ms[str(s)] = t * 1e3
         if t < best_t * 0.98:
             best_s, best_t = s, t
-    tun = Tuning(grids, best_s, {"class_ms_by_grid": per, "build_ms_by_streams": stream_ms})
+    # with several streams the classes share the GPU: one grid size for every class,
+    # timed as whole builds, may beat the per-class choice made one class at a time
+    grid_ms = {}
+    if best_s > 1:
+        for g in candidates:
+            Tuning([g] * _native.NCLASS, best_s).apply(ctx)
+            t = _time_build(ctx, dP, tol, fp32_below, reps)
+            grid_ms[str(g)] = t * 1e3
+            if t < best_t * 0.98:
+                grids, best_t = [g] * _native.NCLASS, t
+    tun = Tuning(grids, best_s, {"class_ms_by_grid": per, "build_ms_by_streams": stream_ms,
+                                 "build_ms_by_grid_with_streams": grid_ms})
     tun.apply(ctx)
     if use_cache:
         os.makedirs(os.path.dirname(CACHE), exist_ok=True)

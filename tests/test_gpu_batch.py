@@ -46,7 +46,7 @@ def test_fock_graph_replay_and_tuning():
     dP = torch.tensor(rng.standard_normal(ctx.nn), device="cuda")
     ref = ctx.fock(dP, tol=1e-12).clone()
     tun = autotune.autotune(ctx, dP, tol=1e-12, reps=1, use_cache=False)
-    assert tun.streams in (1, 2, 4)
+    assert tun.streams in (1, 2, 4, 8)
     assert torch.max(torch.abs(ctx.fock(dP, tol=1e-12) - ref)).item() < 1e-12
     G = torch.empty_like(dP)
     for k in range(3):  # capture, then replays with new contents of the same buffers
