@@ -3,9 +3,10 @@
 // dE/dR_A = 2 sum_ij P_ij dH_ij/dR_A - 2 sum_ij W_ij dS_ij/dR_A
 //         + sum_ijkl (2 P_ij P_kl - P_ik P_jl) d(ij|kl)/dR_A + dV_nn/dR_A
 // with W = P F P, the reference's expression (mmd/forces.py:61-97, P = C_occ C_occ^T),
-// evaluated without ever forming a derivative-integral tensor: every thread computes
-// the derivative integrals of one shell pair (one-electron terms) or one unique shell
-// quartet (two-electron terms) and contracts them at once with the densities.
+// evaluated without ever forming a derivative-integral tensor: a thread computes the
+// derivative integrals of one shell pair and nucleus (one-electron terms), a warp those
+// of one unique shell quartet (two-electron terms), and both contract them at once
+// with the densities.
 //
 // Derivatives of a Cartesian Gaussian with respect to its centre (cython/grad.pyx:
 // 101-108): d/dA_x G_i = 2a G_{i+1} - i G_{i-1}, so the Hermite coefficients of a
@@ -16,7 +17,7 @@
 // nucleus C (its Hellmann-Feynman term).
 //
 // These kernels are generic (runtime loops over angular momenta, s..d shells, total
-// angular momentum up to 9), one launch per gradient; the Boys function comes from its
+// angular momentum up to 9), one launch each per gradient; the Boys function comes from its
 // defining series (downward recursion) below T = 35 and from upward recursion off
 // F_0 = sqrt(pi/T)/2 erf(sqrt T) above.
 #include <cuda_runtime.h>
