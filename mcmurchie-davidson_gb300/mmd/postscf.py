@@ -10,9 +10,14 @@ core Hamiltonian ``Hp`` and orbital energies ``fs`` -- the attributes the refere
 sets, as host arrays.  ``MP2`` evaluates the reference's sums (spatial, and spin-orbital from
 <ij||ab>) as vectorised device reductions instead of Python loops.
 
-The reference's configuration-interaction and response methods (CIS, CISD, FCI,
-TDHF) are consumers of these integrals outside the two-electron hot path and are
-not provided here.
+``CIS`` and ``TDHF`` (mmd/postscf.py:249-400) build the singles matrices A and B from
+device blocks of <AB||CD> and diagonalise on the GPU: CIS energies and oscillator
+strengths from one symmetric eigensolve; TDHF by the reference's three algorithms
+('hermitian': sqrt(A-B)(A+B)sqrt(A-B), the square root from a symmetric
+eigendecomposition; 'reduced': the non-symmetric (A-B)(A+B); 'full': the
+non-symmetric [[A, B], [-B^T, -A^T]]).  The determinant-string paths (CIS with
+``bitstring=True``, CISD, FCI) build Slater-determinant Hamiltonians from bit
+strings, not integral contractions, and are not provided.
 """
 from __future__ import annotations
 
@@ -109,17 +114,92 @@ class PostSCF:
             mol.emp2 = np.complex128(float((num / d).sum().item()) + mol.energy)
         print("E(MP2) = ", mol.emp2.real)
 
-    def _absent(self, name):
-        raise NotImplementedError(f"PostSCF.{name} is not part of this implementation (two-electron hot path only)")
+    def _singles(self, with_b=False):
+        """The singles matrices of mmd/postscf.py:262-266 and 349-355 on the device:
+        A[ia,jb] = (e_a - e_i) d_ij d_ab + <aj||ib>, B[ia,jb] = <ab||ij>."""
+        mol = self.mol
+        torch = mol.context.torch
+        dev = self._mo.device
+        no, nv = mol.nelec, mol.norb - mol.nelec
+        occ, vir = range(0, no), range(no, mol.norb)
+        e = torch.as_tensor(np.diag(mol.fs).copy(), dtype=torch.float64, device=dev)
+        A = self._spin_block(vir, occ, occ, vir).permute(2, 0, 1, 3).reshape(no * nv, no * nv)
+        A = A + torch.diag((e[no:][None, :] - e[:no][:, None]).reshape(-1))
+        if not with_b:
+            return A
+        B = self._spin_block(vir, vir, occ, occ).permute(2, 0, 3, 1).reshape(no * nv, no * nv)
+        return A, B
 
-    def CIS(self, *a, **k):
-        self._absent("CIS")
+    def CIS(self, bitstring=False):
+        """Configuration interaction singles from the RHF reference (mmd/postscf.py:249-322):
+        excitation energies (eV) in ``mol.cis_omega``, oscillator strengths
+        f = 2/3 w |<0|mu|n>|^2 in ``mol.cis_oscil``."""
+        if bitstring:
+            raise NotImplementedError("PostSCF.CIS(bitstring=True) builds a determinant Hamiltonian; "
+                                      "not part of this implementation")
+        mol = self.mol
+        torch = mol.context.torch
+        no, nv = mol.nelec, mol.norb - mol.nelec
+        nOV = no * nv
+        if nOV > 5000:
+            print("Number determinants: ", nOV)
+            sys.exit("CIS too expensive. Quitting.")
+        A = self._singles()
+        print("Diagonalizing Hamiltonian...")
+        w, V = torch.linalg.eigh(A)
+        # MO dipole integrals, spin-blocked (mmd/postscf.py:295-299)
+        C = torch.as_tensor(np.real(np.asarray(mol.C)), dtype=torch.float64, device=A.device)
+        Mmo = C.T @ mol._dev["M"].to(torch.float64) @ C
+        sp = torch.arange(mol.norb, device=A.device)
+        Ms = Mmo[:, sp // 2][:, :, sp // 2] * (sp[:, None] % 2 == sp[None, :] % 2).to(torch.float64)
+        D = Ms[:, :no, no:].reshape(3, nOV)
+        td = D @ V                                                    # (3, states)
+        f = (2.0 / 3.0) * w * (td * td).sum(0)
+        mol.cis_omega = (w * 27.211399).cpu().numpy()
+        mol.cis_oscil = f.cpu().numpy()
+        print("\nConfiguration Interaction Singles (CIS)")
+        print("------------------------------")
+        print("# Determinants: ", nOV)
+        print("nOcc * nVirt:   ", nOV)
+        for state in range(min(nOV, 30)):
+            print("CIS state %2s (eV): %12.4f (f=%6.4f)" % (state + 1, mol.cis_omega[state], mol.cis_oscil[state]))
+
+    def TDHF(self, alg="hermitian"):
+        """Time-dependent Hartree-Fock (RPA) excitation energies in eV, ``mol.tdhf_omega``
+        (mmd/postscf.py:325-400), by the algorithm ``alg`` names."""
+        mol = self.mol
+        torch = mol.context.torch
+        A, B = self._singles(with_b=True)
+        nOV = A.shape[0]
+        if alg == "hermitian":
+            # principal square root of the symmetric positive-definite A - B
+            lam, U = torch.linalg.eigh(A - B)
+            root = (U * lam.sqrt()) @ U.T
+            H = root @ (A + B) @ root
+            w = torch.linalg.eigvalsh(0.5 * (H + H.T)).sqrt()
+        elif alg == "reduced":
+            H = (A - B) @ (A + B)
+            w = torch.sort(torch.linalg.eigvals(H).sqrt().real).values
+        elif alg == "full":
+            H = torch.cat([torch.cat([A, B], 1), torch.cat([-B.T, -A.T], 1)], 0)
+            lam = torch.linalg.eigvals(H)
+            w = torch.sort(lam.real).values[nOV:]
+        else:
+            raise ValueError("alg must be 'hermitian', 'reduced' or 'full'")
+        mol.tdhf_omega = (w * 27.211399).cpu().numpy()
+        print("\nTime-dependent Hartree-Fock (TDHF)")
+        print("------------------------------")
+        print("Algorithm:        ", alg)
+        print("Matrix shape:     ", len(H))
+        print("2 * nOcc * nVirt: ", 2 * nOV)
+        for state in range(min(nOV, 10)):
+            print("TDHF state %2s (eV): %12.4f" % (state + 1, mol.tdhf_omega[state]))
+
+    def _absent(self, name):
+        raise NotImplementedError(f"PostSCF.{name} is not part of this implementation (determinant-string method)")
 
     def CISD(self, *a, **k):
         self._absent("CISD")
 
     def FCI(self, *a, **k):
         self._absent("FCI")
-
-    def TDHF(self, *a, **k):
-        self._absent("TDHF")
