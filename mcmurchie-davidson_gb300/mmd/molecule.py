@@ -193,8 +193,17 @@ class Molecule(SCF, Forces):
     # ---------------------------------------------------------------- integrals
     @property
     def context(self):
-        """Device context of this molecule's basis (pairs, Schwarz table)."""
-        return context_for(self.bfs)
+        """Device context of this molecule's basis (pairs, Schwarz table).  The lookup
+        by basis fingerprint (a pass over every function) runs once per ``bfs`` list;
+        later accesses reuse the context while the list is the same object of the same
+        length (``formBasis`` makes a new list, hence a new lookup)."""
+        bfs = self.bfs
+        ref = self.__dict__.get("_context_ref")
+        if ref is not None and ref[0] is bfs and ref[1] == len(bfs):
+            return ref[2]
+        ctx = context_for(bfs)
+        self._context_ref = (bfs, len(bfs), ctx)
+        return ctx
 
     def build(self, direct=False):
         """One-electron integrals, then the Schwarz table (direct) or the ERI tensor (molecule.py:90-102)."""
