@@ -266,6 +266,18 @@ struct QuartetInfo {
 
 __device__ __forceinline__ int tri(int i) { return i * (i + 1) / 2; }
 
+// |x| of a double as a float rounded toward zero, from its bit pattern on the integer
+// pipe (no FP64 instruction): exponent rebiased, top 23 mantissa bits kept; values
+// below the normal float range give 0.  Relative error below 2^-23, far inside the
+// screening test's guard band.
+__device__ __forceinline__ float abs_f32_trunc(double x) {
+  const int hi = __double2hiint(x) & 0x7fffffff;
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int fe = min((hi >> 20) - (1023 - 127), 254);
+  const int m = ((hi & 0xfffff) << 3) | (int)(lo >> 29);
+  return fe <= 0 ? 0.0f : __int_as_float((fe << 23) | m);
+}
+
 // Fock (formPT) digest --------------------------------------------------------------
 struct FockArgs {
   const double* dP;      // packed per-molecule N x N (density difference)
@@ -316,17 +328,20 @@ struct FockDigest {
     }
     const long long rI = base + (long long)i * N, rJ = base + (long long)j * N;
     const long long rK = base + (long long)k * N;
+    // the six density elements, loaded once for the screening test and the scatter
+    const double* dP = f.dP;
+    const double d_ij = __ldg(dP + rI + j), d_kl = __ldg(dP + rK + l), d_ik = __ldg(dP + rI + k);
+    const double d_il = __ldg(dP + rI + l), d_jk = __ldg(dP + rJ + k), d_jl = __ldg(dP + rJ + l);
     // screening: sqrt(screen[ij]) sqrt(screen[kl]) max(4|dP_ij|,4|dP_kl|,|dP_ik|,|dP_il|,|dP_jk|,|dP_jl|) < tol
     {
-      float dm = fmaxf(4.0f * fmaxf(__ldg(f.dPf + rI + j), __ldg(f.dPf + rK + l)),
-                       fmaxf(fmaxf(__ldg(f.dPf + rI + k), __ldg(f.dPf + rI + l)),
-                             fmaxf(__ldg(f.dPf + rJ + k), __ldg(f.dPf + rJ + l))));
+      float dm = fmaxf(4.0f * fmaxf(abs_f32_trunc(d_ij), abs_f32_trunc(d_kl)),
+                       fmaxf(fmaxf(abs_f32_trunc(d_ik), abs_f32_trunc(d_il)),
+                             fmaxf(abs_f32_trunc(d_jk), abs_f32_trunc(d_jl))));
       const float bf = __ldg(f.sqf + tbase + ij) * __ldg(f.sqf + tbase + kl) * dm;
       if (bf < f.tolf_lo) return;
       if (bf < f.tolf_hi) {  // near the threshold: the reference's test in FP64
-        const double* dP = f.dP;
-        double d = fmax(4.0 * fmax(fabs(dP[rI + j]), fabs(dP[rK + l])),
-                        fmax(fmax(fabs(dP[rI + k]), fabs(dP[rI + l])), fmax(fabs(dP[rJ + k]), fabs(dP[rJ + l]))));
+        double d = fmax(4.0 * fmax(fabs(d_ij), fabs(d_kl)),
+                        fmax(fmax(fabs(d_ik), fabs(d_il)), fmax(fabs(d_jk), fabs(d_jl))));
         if (f.sq[tbase + ij] * f.sq[tbase + kl] * d < f.tol) return;
       }
     }
@@ -339,14 +354,13 @@ struct FockDigest {
     const long long deg = (long long)((i != j) + (k != l) + !(i == k && j == l));
     const double v = __longlong_as_double(bits + (deg << 52));
     const double vq = __longlong_as_double((bits + ((deg - 2) << 52)) ^ (long long)0x8000000000000000ULL);
-    const double* dP = f.dP;
     double* G = f.G;
-    atomicAdd(G + rI + j, dP[rK + l] * v);
-    atomicAdd(G + rK + l, dP[rI + j] * v);
-    atomicAdd(G + rI + k, dP[rJ + l] * vq);
-    atomicAdd(G + rJ + l, dP[rI + k] * vq);
-    atomicAdd(G + rI + l, dP[rJ + k] * vq);
-    atomicAdd(G + rK + j, dP[rI + l] * vq);
+    atomicAdd(G + rI + j, d_kl * v);
+    atomicAdd(G + rK + l, d_ij * v);
+    atomicAdd(G + rI + k, d_jl * vq);
+    atomicAdd(G + rJ + l, d_ik * vq);
+    atomicAdd(G + rI + l, d_jk * vq);
+    atomicAdd(G + rK + j, d_il * vq);
     ++nfq;
   }
 };
