@@ -51,9 +51,9 @@ FQ_PER_BUILD = 198282802.0
 # DRAM bytes (read + write) of one launch of the top class kernels in the first, full
 # Fock build of this workload, from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum; summary and command in profiles/k_fock_fp64_pipe_h2o16.md).
-DRAM_BYTES_PER_LAUNCH = {"1000": 47.75e6, "0000": 24.0e6, "1010": 25.4e6, "1110": 16.0e6, "2111": 5.3e6}
+DRAM_BYTES_PER_LAUNCH = {"1000": 47.3e6, "0000": 23.9e6, "1010": 25.0e6, "1110": 15.6e6, "2111": 4.9e6}
 # FP64-pipe busy fraction of the same launches (sm__pipe_fp64_cycles_active, same capture)
-FP64_PIPE_BUSY = {"1000": 0.730, "0000": 0.546, "1010": 0.686, "1110": 0.562, "2111": 0.678}
+FP64_PIPE_BUSY = {"1000": 0.733, "0000": 0.545, "1010": 0.694, "1110": 0.573, "2111": 0.714}
 
 
 def _env():
