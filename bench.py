@@ -371,6 +371,9 @@ def _polished_energy(mol):
 # within 2e-12 Eh of the FP64 oracle, while moving more quartets off the FP64 pipe.
 # The mixed-precision report on (H2O)32 (mixed_bench) keeps 1e-5.
 COMBINED_FP32_BELOW = 1e-3
+# time-to-converge figures of the benchmark molecule: best of this many end-to-end runs
+# (fresh device context each), plain path and chosen form alike
+TTC_RUNS = 2
 
 
 def combined_bench(nmol=64, thr=COMBINED_FP32_BELOW, conver=1e-8):
@@ -593,21 +596,26 @@ def gpu_arm(args):
     del G
     e2e = {"value": world * len(Ph) / t_e2e, "unit": "Fock builds/s", "api": "mmd.integrals.fock.formPT (host arrays)",
            "h2d_bytes_per_step": N * N * 8, "d2h_bytes_per_step": N * N * 8}
-    # ---------------- time to converge through Molecule(...).RHF (fresh device context)
+    # ---------------- time to converge through Molecule(...).RHF (fresh device context),
+    # best of TTC_RUNS runs for the plain path and for the chosen form alike
     ttc, E, iters = None, None, None
     if not args.no_ttc:
         from mmd.integrals import twoe
-        twoe._ctx_cache.clear()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        m2 = Molecule(geom, "6-31gss")
-        E = float(m2.RHF(doPrint=False, direct=True, fp32_below=fp32))
-        ttc = time.perf_counter() - t0
-        iters = int(m2.iterations)
+        for _ in range(TTC_RUNS):
+            twoe._ctx_cache.clear()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            m_ = Molecule(geom, "6-31gss")
+            E_ = float(m_.RHF(doPrint=False, direct=True, fp32_below=fp32))
+            t_ = time.perf_counter() - t0
+            if ttc is None or t_ < ttc:
+                ttc, E, iters, m2 = t_, E_, int(m_.iterations), m_
     chosen = None
     if not args.no_ttc and rank == 0 and fp32 == 0.0:
         try:
-            chosen = chosen_form_ttc(geom, ttc, iters, m2)
+            runs = [chosen_form_ttc(geom, ttc, iters, m2) for _ in range(TTC_RUNS)]
+            chosen = min(runs, key=lambda r: r["time_to_converge_s"])
+            chosen["runs"] = TTC_RUNS
         except Exception as e:  # reported, never required for the headline
             chosen = {"error": str(e)[:300]}
     # ---------------- CPU baseline (rank 0, N = 1)
@@ -654,7 +662,8 @@ def gpu_arm(args):
         "config": dict(WORKLOAD, fp32_below=fp32, l2="flushed between steps (512 MB write)",
                        fq_per_build=fq_per_build, eris_per_s=fq_per_build * value / world,
                        parallelism="replicas" if world > 1 else "single GPU"),
-        "e2e": e2e, "time_to_converge_s": ttc, "scf_iterations": iters, "energy": E, "chosen_form": chosen,
+        "e2e": e2e, "time_to_converge_s": ttc, "ttc_runs": TTC_RUNS, "scf_iterations": iters, "energy": E,
+        "chosen_form": chosen,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches_per_build * builds, "wall_s": wall,
         "step_breakdown_ms": {"step": 1e3 * t_dev / builds, "fock_class_kernels_one_stream": build_ms,
