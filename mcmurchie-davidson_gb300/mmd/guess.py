@@ -144,40 +144,52 @@ def molecule_layout(mol, gb: GuessBasis = B631G):
 
 
 def pair_features(Z, X, R):
-    """Ordered pairs (A <= B) within the cutoff and their feature rows."""
+    """Ordered pairs (A <= B) within the cutoff and their feature rows: element-pair
+    one-hot (or the element of a diagonal block), the distance on 32 Gaussians, the
+    bond direction in each atom's local frame, and the relative frame orientation."""
     n = len(Z)
-    pairs, rows = [], []
-    for a in range(n):
-        for b in range(a, n):
-            v = X[b] - X[a]
-            d = float(np.linalg.norm(v))
-            if d > CUTOFF:
-                continue
-            f = np.zeros(NIN)
-            if a == b:
-                f[4 if Z[a] == 8 else 5] = 1.0
-            else:
-                f[TYPES[(int(Z[a]), int(Z[b]))]] = 1.0
-                f[38:41] = R[a] @ (v / d)
-                f[41:44] = R[b] @ (-v / d)
-            f[6:38] = np.exp(-((d - RBF_CENTERS) / RBF_WIDTH) ** 2)
-            f[44:53] = (R[a] @ R[b].T).ravel()
-            pairs.append((a, b))
-            rows.append(f)
-    return pairs, np.array(rows, dtype=np.float32)
+    Z = np.asarray(Z).astype(int)
+    ia, ib = np.triu_indices(n)                       # a <= b, row-major: (0,0), (0,1), ...
+    v = X[ib] - X[ia]
+    d = np.linalg.norm(v, axis=1)
+    keep = d <= CUTOFF
+    ia, ib, v, d = ia[keep], ib[keep], v[keep], d[keep]
+    diag = ia == ib
+    F = np.zeros((len(ia), NIN))
+    rows = np.arange(len(ia))
+    tcol = np.array([TYPES[(int(za), int(zb))] for za, zb in zip(Z[ia], Z[ib])], dtype=int) if len(ia) else \
+        np.zeros(0, dtype=int)
+    dcol = np.where(Z[ia] == 8, 4, 5)
+    F[rows, np.where(diag, dcol, tcol)] = 1.0
+    off = ~diag
+    u = np.zeros_like(v)
+    u[off] = v[off] / d[off, None]
+    F[off, 38:41] = np.einsum("pij,pj->pi", R[ia[off]], u[off])
+    F[off, 41:44] = np.einsum("pij,pj->pi", R[ib[off]], -u[off])
+    F[:, 6:38] = np.exp(-((d[:, None] - RBF_CENTERS[None, :]) / RBF_WIDTH) ** 2)
+    F[:, 44:53] = np.einsum("pik,pjk->pij", R[ia], R[ib]).reshape(-1, 9)
+    pairs = list(zip(ia.tolist(), ib.tolist()))
+    return pairs, F.astype(np.float32)
+
+
+def _atom_transforms(Z, R, gb: GuessBasis, local: bool = False):
+    """block_transform of every atom (its inverse transpose with ``local`` for a basis
+    with d functions), computed once per atom rather than once per pair."""
+    T = [block_transform(int(z), r, gb) for z, r in zip(Z, R)]
+    if local and gb.has_d:
+        T = [_to_local(t) for t in T]
+    return T
 
 
 def pair_targets(P, Z, R, off, pairs, gb: GuessBasis = B631G):
     nm = gb.nmax
     Y = np.zeros((len(pairs), gb.nout), dtype=np.float32)
     M = np.zeros((len(pairs), gb.nout), dtype=np.float32)
+    T = _atom_transforms(Z, R, gb, local=True)
     for k, (a, b) in enumerate(pairs):
         na, nb = gb.nfunc[int(Z[a])], gb.nfunc[int(Z[b])]
         blk = P[off[a]:off[a] + na, off[b]:off[b] + nb]
-        Ta, Tb = block_transform(int(Z[a]), R[a], gb), block_transform(int(Z[b]), R[b], gb)
-        if gb.has_d:
-            Ta, Tb = _to_local(Ta), _to_local(Tb)
-        loc = Ta @ blk @ Tb.T
+        loc = T[a] @ blk @ T[b].T
         t = np.zeros((nm, nm))
         m = np.zeros((nm, nm))
         t[:na, :nb] = loc
@@ -188,12 +200,15 @@ def pair_targets(P, Z, R, off, pairs, gb: GuessBasis = B631G):
 
 
 def assemble(pred, Z, R, off, pairs, N, gb: GuessBasis = B631G):
+    """Lab-frame density from the predicted local-frame blocks: P[A,B] = T_A^T P' T_B
+    (diagonal blocks symmetrised, P[B,A] = P[A,B]^T)."""
     nm = gb.nmax
     P = np.zeros((N, N))
+    T = _atom_transforms(Z, R, gb)
     for k, (a, b) in enumerate(pairs):
         na, nb = gb.nfunc[int(Z[a])], gb.nfunc[int(Z[b])]
         loc = pred[k].reshape(nm, nm)[:na, :nb]
-        blk = block_transform(int(Z[a]), R[a], gb).T @ loc @ block_transform(int(Z[b]), R[b], gb)
+        blk = T[a].T @ loc @ T[b]
         if a == b:
             blk = 0.5 * (blk + blk.T)
         P[off[a]:off[a] + na, off[b]:off[b] + nb] = blk
