@@ -5,7 +5,9 @@
   good to ~7e-10 relative) and an mpmath grid (relative 5e-15);
 * contracted ERIs of every angular class, the full water/STO-3G tensor and the
   Schwarz tables: the compiled reference, run to make the fixtures;
-* formPT: the reference's own recorded calls (inputs and unsymmetrised output).
+* formPT: the reference's own recorded calls (inputs and unsymmetrised output);
+* the excited-state chain (RHF, spin-orbital integrals, CIS, TDHF): the reference's
+  own excitation energies.
 """
 import json
 import os
@@ -106,3 +108,21 @@ def test_formPT_records(golden, name):
         assert np.max(np.abs(G.real - d[f"formPT{k}_G"])) < 1e-13
         k += 1
     assert k >= 1
+
+
+def test_excited_state_oracle_matches_reference():
+    """The CPU restatement of the reference's RHF -> CIS / TDHF chain (oracle/
+    postscf_oracle.py), started from the golden integrals of water 3-21G and STO-3G,
+    reproduces the reference's own excitation energies (tests/golden/excited.json)."""
+    import postscf_oracle as X
+    with open(os.path.join(GOLDEN, "excited.json")) as f:
+        gold = json.load(f)
+    for case, key in ((("cis",), "mol_water_321g.npz"), (("tdhf",), "mol_water_sto3g.npz")):
+        d = np.load(os.path.join(GOLDEN, key))
+        C, e = X.rhf(d["S"], d["T"], d["V"], d["TwoE"], int(d["nocc"]))
+        A, B = X.singles(e, X.spin_integrals(C, d["TwoE"]), 2 * int(d["nocc"]))
+        if case[0] == "cis":
+            assert np.abs(X.cis(A) - np.asarray(gold["cis"]["omega"])).max() < 1e-9   # eV
+        else:
+            for alg in ("hermitian", "reduced", "full"):
+                assert np.abs(X.tdhf(A, B, alg) - np.asarray(gold["tdhf"][alg])).max() < 1e-9
