@@ -1,13 +1,14 @@
-"""CPU oracle of the excited-state consumers (TEST INFRASTRUCTURE ONLY).
+"""CPU oracle of the post-SCF consumers: MP2, CIS, TDHF (TEST INFRASTRUCTURE ONLY).
 
 A float64 numpy restatement of what the reference computes after a conventional
 RHF: the RHF itself (mmd/scf.py:10-80: P = C_occ C_occ^T without the factor 2,
 F = H + 2J - K, DIIS on the orthogonalised commutator, stop on ||P - P_old||_F),
 the spin-orbital integrals <pq||rs> of ``ao2mo`` (mmd/postscf.py:21-41; spin orbital
-2p + sigma), the CIS matrix A (mmd/postscf.py:249-267) and the three TDHF
+2p + sigma), the MP2 correlation energies (mmd/postscf.py:44-73, spatial and
+spin-orbital), the CIS matrix A (mmd/postscf.py:249-267) and the three TDHF
 eigenproblems (mmd/postscf.py:325-381).  It starts from the one- and two-electron
 integrals of the golden fixtures, so it runs without a GPU; the GPU PostSCF is
-checked against the reference's own excitation energies directly.
+checked against the reference's own MP2 and excitation energies directly.
 """
 import numpy as np
 import scipy.linalg
@@ -61,6 +62,24 @@ def spin_integrals(C, TwoE):
     phys = mo[np.ix_(sp, sp, sp, sp)].transpose(0, 2, 1, 3)          # <pq|rs> = (pr|qs) spatially
     coul = phys * same[:, None, :, None] * same[None, :, None, :]
     return coul - coul.transpose(0, 1, 3, 2)
+
+
+def mp2_spatial(C, e_mo, TwoE, nocc):
+    """Sum_ijab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b)."""
+    mo = np.einsum("pqrs,pP,qQ,rR,sS->PQRS", TwoE, C, C, C, C, optimize=True)
+    o, v = slice(0, nocc), slice(nocc, len(e_mo))
+    iajb = mo[o, v, o, v]
+    d = e_mo[o][:, None, None, None] - e_mo[v][None, :, None, None] + e_mo[o][None, None, :, None] - \
+        e_mo[v][None, None, None, :]
+    return float(np.sum(iajb * (2.0 * iajb - iajb.transpose(0, 3, 2, 1)) / d))
+
+
+def mp2_spin(e_mo, dbl, nelec):
+    """(1/4) Sum_ijab |<ij||ab>|^2 / (e_i + e_j - e_a - e_b) over spin orbitals."""
+    e = np.repeat(e_mo, 2)
+    o, v = slice(0, nelec), slice(nelec, len(e))
+    d = e[o][:, None, None, None] + e[o][None, :, None, None] - e[v][None, None, :, None] - e[v][None, None, None, :]
+    return float(0.25 * np.sum(dbl[o, o, v, v] ** 2 / d))
 
 
 def singles(e_mo, dbl, nelec):

@@ -126,3 +126,19 @@ def test_excited_state_oracle_matches_reference():
         else:
             for alg in ("hermitian", "reduced", "full"):
                 assert np.abs(X.tdhf(A, B, alg) - np.asarray(gold["tdhf"][alg])).max() < 1e-9
+
+
+def test_mp2_oracle_matches_reference():
+    """MP2 (spatial and spin-orbital) of the CPU restatement from the golden integrals
+    equals the reference's own MP2 energies (tests/golden/mp2.json) for water STO-3G
+    and 6-31G."""
+    import postscf_oracle as X
+    with open(os.path.join(GOLDEN, "mp2.json")) as f:
+        cases = {(c["name"], c["basis"]): c for c in json.load(f)["cases"]}
+    for key, fixture in ((("water", "sto-3g"), "mol_water_sto3g.npz"), (("water", "6-31g"), "mol_water_631g.npz")):
+        d, c = np.load(os.path.join(GOLDEN, fixture)), cases[key]
+        nocc = int(d["nocc"])
+        C, e = X.rhf(d["S"], d["T"], d["V"], d["TwoE"], nocc)
+        assert abs(X.mp2_spatial(C, e, d["TwoE"], nocc) + c["energy"] - c["emp2_spatial"]) < 1e-10
+        dbl = X.spin_integrals(C, d["TwoE"])
+        assert abs(X.mp2_spin(e, dbl, 2 * nocc) + c["energy"] - c["emp2_spin"]) < 1e-10
