@@ -48,3 +48,27 @@ def test_single_process_needs_no_group():
     import bench
     assert bench.max_over_ranks(3.5) == 3.5
     assert bench.replica_throughput(1, 20, 2.0) == 10.0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """``bench.py --impl reference`` (the reference's own compiled formPT on the host
+    cores; no GPU) prints one JSON line with the GPU arm's metric, unit and config and
+    an e2e object without host-device traffic."""
+    import json
+    import subprocess
+    if not os.path.isdir(os.path.join(ROOT, "oracle", "_ref", "mmd")):
+        pytest.skip("the reference's compiled Cython (oracle/_ref) is not built here")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    if "unavailable" in line:
+        return
+    import bench
+    assert line["metric"] == bench.METRIC and line["unit"] == "Fock builds/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["config"]["workload"] == bench.WORKLOAD["workload"]
+    assert line["cpu_baseline"]["kind"] == "reference" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
