@@ -12,8 +12,8 @@ Tunables (C ABI ``mmdg_set_tuning`` / ``mmdg_set_streams``):
 
 Each candidate is timed with CUDA events on a representative density difference
 (``mmdg_fock_timed`` per class for the per-class grids, whole builds otherwise).
-Results are cached as JSON under ``_build/tuning.json`` keyed by the GPU name and
-the basis signature (molecules, functions, shells).
+Results are cached as JSON under ``_build/tuning.json`` keyed by the GPU name, the
+basis signature (molecules, functions, shells) and the FP32 threshold.
 """
 from __future__ import annotations
 
@@ -43,10 +43,30 @@ class Tuning:
         return {"grids": self.grids, "streams": self.streams, "measured": self.measured}
 
 
-def _key(ctx):
+def _key(ctx, fp32_below=0.0):
     torch = ctx.torch
     name = torch.cuda.get_device_name(ctx.device)
-    return f"{name}|nmol={ctx.nmol}|nfunc={int(np.sum(ctx.nfunc))}|nshell={ctx.nshell}"
+    return f"{name}|nmol={ctx.nmol}|nfunc={int(np.sum(ctx.nfunc))}|nshell={ctx.nshell}|fp32_below={float(fp32_below):g}"
+
+
+def _load_cache():
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(key, tun):
+    """Adds one entry; the file is replaced atomically (concurrent tuners may lose an
+    entry, never corrupt the file)."""
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    cache = _load_cache()
+    cache[key] = tun.to_json()
+    tmp = f"{CACHE}.{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1)
+    os.replace(tmp, CACHE)
 
 
 def _time_build(ctx, dP, tol, split, reps):
@@ -62,15 +82,10 @@ def _time_build(ctx, dP, tol, split, reps):
 
 
 def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuning:
-    key = _key(ctx)
-    cache = {}
-    if use_cache and os.path.exists(CACHE):
-        try:
-            cache = json.load(open(CACHE))
-        except (OSError, ValueError):
-            cache = {}
-        if key in cache:
-            t = cache[key]
+    key = _key(ctx, fp32_below)
+    if use_cache:
+        t = _load_cache().get(key)
+        if t is not None:
             tun = Tuning(t["grids"], t["streams"], t.get("measured"))
             tun.apply(ctx)
             return tun
@@ -115,8 +130,5 @@ def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuni
                                  "build_ms_by_grid_with_streams": grid_ms})
     tun.apply(ctx)
     if use_cache:
-        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
-        cache[key] = tun.to_json()
-        with open(CACHE, "w") as f:
-            json.dump(cache, f, indent=1)
+        _store_cache(key, tun)
     return tun

@@ -142,3 +142,18 @@ def test_single_threaded_blas_scope_restores_the_thread_count():
         w = np.linalg.eigh(np.diag([3.0, 1.0, 2.0]))[0]
     assert ctl[0]() == before
     assert w.tolist() == [1.0, 2.0, 3.0]
+
+
+def test_autotune_cache_round_trip(tmp_path, monkeypatch):
+    """The tuning cache stores one entry per key and survives a corrupt file."""
+    from mmd import autotune
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "tuning.json"))
+    assert autotune._load_cache() == {}
+    autotune._store_cache("gpu|a", autotune.Tuning([0] * 21, 4, {"x": 1}))
+    autotune._store_cache("gpu|b", autotune.Tuning([152] * 21, 1))
+    c = autotune._load_cache()
+    assert c["gpu|a"]["streams"] == 4 and c["gpu|a"]["measured"] == {"x": 1}
+    assert c["gpu|b"]["grids"] == [152] * 21
+    (tmp_path / "tuning.json").write_text("{not json")
+    assert autotune._load_cache() == {}
+    assert not list(tmp_path.glob("*.tmp"))
