@@ -157,3 +157,38 @@ def test_autotune_cache_round_trip(tmp_path, monkeypatch):
     (tmp_path / "tuning.json").write_text("{not json")
     assert autotune._load_cache() == {}
     assert not list(tmp_path.glob("*.tmp"))
+
+
+def test_batch_padding_and_host_eigensolves():
+    """The batched SCF's packed <-> padded density maps and its per-molecule host
+    eigensolves (thread pool, converged molecules skipped) on CPU tensors."""
+    import types
+    import torch
+    from mmd import batch
+    N = np.array([3, 5, 2])
+    br = object.__new__(batch.BatchRHF)
+    br.torch, br.dev, br.N, br.B, br.Nmax = torch, "cpu", N, len(N), int(N.max())
+    base = np.concatenate([[0], np.cumsum(N ** 2)[:-1]])
+    br.ctx = types.SimpleNamespace(nn=int(np.sum(N ** 2)))
+    pk, pd = [], []
+    for b, n in enumerate(N):
+        i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+        pk.append(base[b] + (i * n + j).ravel())
+        pd.append(b * br.Nmax ** 2 + (i * br.Nmax + j).ravel())
+    br.pk, br.pd = torch.as_tensor(np.concatenate(pk)), torch.as_tensor(np.concatenate(pd))
+    rng = np.random.default_rng(3)
+    packed = torch.as_tensor(rng.standard_normal(br.ctx.nn))
+    padded = br._pad(packed)
+    assert padded.shape == (3, 5, 5)
+    assert torch.equal(padded[1, :5, :5].reshape(-1), packed[9:34])
+    assert float(padded[0, 3:, :].abs().sum()) == 0.0 and float(padded[2, :, 2:].abs().sum()) == 0.0
+    assert torch.equal(br._pack(padded), packed)
+    sym = padded + padded.transpose(1, 2)
+    E, C = br._eigh(sym, active=np.array([True, False, True]))
+    for b in (0, 2):
+        n = N[b]
+        w = np.linalg.eigvalsh(sym[b, :n, :n].numpy())
+        assert np.abs(E[b, :n].numpy() - w).max() < 1e-12
+        V = C[b, :n, :n].numpy()
+        assert np.abs(sym[b, :n, :n].numpy() @ V - V * E[b, :n].numpy()).max() < 1e-12
+    assert float(E[1].abs().sum()) == 0.0 and float(C[1].abs().sum()) == 0.0
