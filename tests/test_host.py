@@ -192,3 +192,47 @@ def test_batch_padding_and_host_eigensolves():
         V = C[b, :n, :n].numpy()
         assert np.abs(sym[b, :n, :n].numpy() @ V - V * E[b, :n].numpy()).max() < 1e-12
     assert float(E[1].abs().sum()) == 0.0 and float(C[1].abs().sum()) == 0.0
+
+
+def test_diis_extrapolation_matches_the_reference_formula():
+    """SCF._diis (device tensors, host (n+1)^2 solve) against a numpy restatement of
+    the reference's updateDIIS (mmd/scf.py:146-180): error X (FPS - SPF) X, B_ij =
+    tr(e_i^T e_j), an 8-deep window, F = sum_i w_i F_i; run on CPU tensors."""
+    import types
+    import torch
+    from mmd.scf import SCF
+    rng = np.random.default_rng(11)
+    n = 6
+    A = rng.standard_normal((n, n))
+    S = A @ A.T + n * np.eye(n)
+    w, U = np.linalg.eigh(S)
+    X = (U / np.sqrt(w)) @ U.T
+    P = rng.standard_normal((n, n))
+    P = P + P.T
+    fake = types.SimpleNamespace(context=types.SimpleNamespace(torch=torch))
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64)
+    fs, es, rf, re_ = [], [], [], []
+    for k in range(11):
+        F = rng.standard_normal((n, n))
+        F = F + F.T
+        Fd, err = SCF._diis(fake, t(F), t(P), t(S), t(X), fs, es)
+        # the reference's algorithm
+        e = X @ (F @ P @ S - S @ P @ F) @ X
+        rf.append(F)
+        re_.append(e)
+        if len(rf) > 8:
+            del rf[0], re_[0]
+        m = len(rf)
+        B = np.zeros((m + 1, m + 1))
+        B[-1, :] = B[:, -1] = -1.0
+        B[-1, -1] = 0.0
+        for i in range(m):
+            for j in range(i + 1):
+                B[i, j] = B[j, i] = np.trace(re_[i].T @ re_[j])
+        r = np.zeros(m + 1)
+        r[-1] = -1.0
+        wts = np.linalg.solve(B, r)
+        Fref = sum(wts[i] * rf[i] for i in range(m))
+        assert len(fs) == m
+        assert np.abs(Fd.numpy() - Fref).max() < 1e-10 * max(1.0, np.abs(Fref).max())
+        assert abs(err - np.linalg.norm(e)) < 1e-10 * max(1.0, np.linalg.norm(e))
