@@ -236,3 +236,29 @@ def test_diis_extrapolation_matches_the_reference_formula():
         assert len(fs) == m
         assert np.abs(Fd.numpy() - Fref).max() < 1e-10 * max(1.0, np.abs(Fref).max())
         assert abs(err - np.linalg.norm(e)) < 1e-10 * max(1.0, np.linalg.norm(e))
+
+
+def test_save_integrals_writes_the_crawford_files(golden, tmp_path):
+    """Molecule.save_integrals (mmd/molecule.py:295-315): enuc/nbf/nelec/s/t/v.dat,
+    eri.dat as 1-based "i j k l value" lines over all N^4 indices, geometry.txt; the
+    arrays read back equal the golden water/STO-3G integrals."""
+    from mmd.molecule import Molecule
+    d = golden("mol_water_sto3g.npz")
+    m = Molecule(str(d["geometry"]), "sto-3g")
+    m.S, m.T, m.V, m.TwoE = d["S"], d["T"], d["V"], d["TwoE"]
+    m.nuc_energy = float(d["nuc_energy"])
+    m.is_built = True
+    out = str(tmp_path / "ints")
+    m.save_integrals(out)
+    N = m.nbasis
+    assert float(np.loadtxt(out + "/enuc.dat")) == float(d["nuc_energy"])
+    assert int(np.loadtxt(out + "/nbf.dat")) == N == 7
+    assert int(np.loadtxt(out + "/nelec.dat")) == 10
+    for name, ref in (("s", d["S"]), ("t", d["T"]), ("v", d["V"])):
+        assert np.abs(np.loadtxt(out + f"/{name}.dat") - ref).max() < 1e-15
+    rows = np.loadtxt(out + "/eri.dat")
+    assert rows.shape == (N ** 4, 5)
+    idx = rows[:, :4].astype(int) - 1
+    assert (idx[:3] == [[0, 0, 0, 0], [0, 0, 0, 1], [0, 0, 0, 2]]).all()
+    assert np.abs(rows[:, 4] - d["TwoE"][idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3]]).max() < 1e-15
+    assert open(out + "/geometry.txt").read().strip() == str(d["geometry"]).strip()
