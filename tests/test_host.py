@@ -1,5 +1,7 @@
 """Host-side logic (CPU): basis parsing and normalisation, shell grouping, clusters,
-flop model and the C-ABI symbol table of libmmdg.so."""
+flop model, the C-ABI symbol table of libmmdg.so, the Boys table, the autotuner
+cache, the batched SCF's padding and host eigensolves, DIIS against the reference's
+formula, and the Crawford-format integral files."""
 import os
 import re
 
