@@ -29,6 +29,9 @@ CACHE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 class Tuning:
+    """A launch schedule: per-class persistent grid (0 = one full wave) and the number
+    of concurrent class streams."""
+
     def __init__(self, grids=None, streams=1, measured=None):
         self.grids = list(grids) if grids is not None else [0] * _native.NCLASS
         self.streams = int(streams)
@@ -82,6 +85,8 @@ def _time_build(ctx, dP, tol, split, reps):
 
 
 def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuning:
+    """Times the candidate schedules on the density difference ``dP`` and applies the
+    fastest to ``ctx`` (cached per GPU, basis signature and FP32 threshold)."""
     key = _key(ctx, fp32_below)
     if use_cache:
         t = _load_cache().get(key)

@@ -65,6 +65,12 @@ class _single_threaded_blas:
 
 
 class BatchRHF:
+    """RHF of many molecules in lockstep through one device context: one Fock build
+    (a CUDA graph of every class's screening and evaluation launch) serves the whole
+    batch per iteration; the dense algebra runs on padded (B, Nmax, Nmax) tensors, the
+    eigensolves on the host cores; molecules that converge drop out of the
+    eigensolves.  ``run`` returns the energies (mmd/scf.py:10-80 per molecule)."""
+
     def __init__(self, geometries, basis="6-31g", acc2e=1e-12, fp32_below=0.0, graph=True, tuning=None):
         torch = _native._torch()
         self.torch = torch

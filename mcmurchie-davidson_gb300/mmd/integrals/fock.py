@@ -19,6 +19,10 @@ def _screen_array(screen, N):
 
 
 def formPT(P, P_old, bfs, nbasis, screen, tol):
+    """Two-electron Fock contribution G(P - P_old), unsymmetrised, as a complex N x N
+    array (cython/fock.pyx:13-87): the reference's Schwarz x density screening of
+    every function quartet at ``tol``, degeneracy factors and scatter, computed by
+    the GPU class kernels (a complex density difference is two real builds)."""
     N = int(nbasis)
     ctx = context_for(bfs)
     torch = ctx.torch

@@ -50,6 +50,7 @@ def comp_norm(lmn) -> float:
 
 @dataclass
 class ShellSet:
+    """The shells of one molecule's basis, in the flat layout mmdg_set_basis takes."""
     nfunc: int
     L: np.ndarray        # [S] int32
     nprim: np.ndarray    # [S] int32
@@ -65,6 +66,10 @@ class ShellSet:
 
 
 def shells_from_bfs(bfs) -> ShellSet:
+    """Groups a reference basis list (one ``Basis`` per Cartesian function,
+    mmd/molecule.py:57-88) into shells: consecutive functions with the same origin,
+    angular momentum, exponents and component-free weights form one shell; any
+    function that does not fit starts a new shell (its other components absent)."""
     L_, K_, cen_, ex_, co_, fn_ = [], [], [], [], [], []
     cur = None  # (origin, L, exps, weights, last component index)
     for f, b in enumerate(bfs):

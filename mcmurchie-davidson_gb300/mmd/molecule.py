@@ -160,12 +160,16 @@ class Molecule(SCF, Forces):
                                             for k in range(3)]) * (1.0 / Z)
 
     def momentum2shell(self, momentum):
+        """Cartesian components of an angular-momentum label, in the reference's
+        order (mmd/molecule.py:104-115)."""
         return SHELLS[str(momentum)]
 
     def sym2num(self, sym):
+        """Atomic number of an element symbol (mmd/molecule.py:117-133)."""
         return SYMBOLS.index(str(sym))
 
     def getBasis(self, filename):
+        """Basis-set data of a .gbs file (mmd/molecule.py:135-189)."""
         return get_basis(filename)
 
     def read_molecule(self, geometry):

@@ -54,9 +54,11 @@ class RealTime:
         self.mol.orthoFock()
 
     def Magnus2(self, direction="x"):
+        """Second-order Magnus propagation along ``direction`` (mmd/realtime.py:32-74)."""
         self._run(2, direction)
 
     def Magnus4(self, direction="x"):
+        """Fourth-order Magnus propagation along ``direction`` (mmd/realtime.py:76-153)."""
         self._run(4, direction)
 
     # ------------------------------------------------------------------ device run

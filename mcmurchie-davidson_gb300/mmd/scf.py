@@ -61,6 +61,13 @@ class SCF(object):
 
     def RHF(self, doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12, fp32_below=0.0, guess=None,
             guess_fallback=True, maxiter=100, polish=False):
+        """Restricted Hartree-Fock (mmd/scf.py:10-80): core-Hamiltonian start (or the
+        density ``guess``, abandoned for the core guess after three growing DIIS
+        errors when ``guess_fallback``), DIIS, stop on ||P - P_old||_F < conver.
+        ``direct``: incremental formPT-semantics Fock builds with Schwarz x density
+        screening at ``acc2e``; ``fp32_below``: shell quartets with Schwarz bound below
+        it in FP32; ``polish``: the returned energy from one non-incremental FP64 build
+        of the final density.  Returns the energy (a numpy float64)."""
         state = self.scf_begin(DIIS=DIIS, direct=direct, acc2e=acc2e, fp32_below=fp32_below, guess=guess,
                                guess_fallback=guess_fallback, maxiter=maxiter)
         t_start = time.perf_counter()
@@ -182,22 +189,29 @@ class SCF(object):
 
     # ---------------------------------------------------------------- reference helpers
     def orthoFock(self):
+        """FO = X^T F X (mmd/scf.py:102-104)."""
         self.FO = np.dot(self.X.T, np.dot(self.F, self.X))
 
     def unOrthoFock(self):
+        """F = U^T FO U (mmd/scf.py:106-108)."""
         self.F = np.dot(self.U.T, np.dot(self.FO, self.U))
 
     def orthoDen(self):
+        """PO = U P U^T (mmd/scf.py:110-112)."""
         self.PO = np.dot(self.U, np.dot(self.P, self.U.T))
 
     def unOrthoDen(self):
+        """P = X PO X^T (mmd/scf.py:114-116)."""
         self.P = np.dot(self.X, np.dot(self.PO, self.X.T))
 
     def computeEnergy(self):
+        """E = tr((H + F) P) + E_nuc (mmd/scf.py:118-121)."""
         self.el_energy = np.einsum("pq,qp", self.Core + self.F, self.P)
         self.energy = self.el_energy + self.nuc_energy
 
     def computeDipole(self):
+        """Dipole in Debye from P and the dipole integrals about the centre of charge
+        (mmd/scf.py:123-129)."""
         self.el_energy = np.einsum("pq,qp", self.Core + self.F, self.P)
         for i in range(3):
             self.mu[i] = -2 * np.trace(np.dot(self.P, self.M[i])) + sum(
@@ -205,10 +219,12 @@ class SCF(object):
         self.mu *= 2.541765
 
     def adj(self, x):
+        """Conjugate transpose of a square matrix (mmd/scf.py:131-134)."""
         assert x.shape[0] == x.shape[1]
         return np.conjugate(x).T
 
     def comm(self, A, B):
+        """[A, B] = AB - BA (mmd/scf.py:136-138)."""
         return np.dot(A, B) - np.dot(B, A)
 
     def buildFock(self):
@@ -240,6 +256,7 @@ class SCF(object):
             self.F = self.Core.astype(complex) + self.G
 
     def updateFock(self):
+        """unOrthoDen, buildFock, orthoFock (mmd/scf.py:140-144)."""
         self.unOrthoDen()
         self.buildFock()
         self.orthoFock()
@@ -280,6 +297,8 @@ class _RHFState:
         self.last_dP = None
 
     def iterate(self):
+        """One SCF pass (mmd/scf.py:30-60): Fock build, DIIS, orthogonalised Fock,
+        eigensolve, new density, energy and ||P - P_old||."""
         mol, torch = self.mol, self.torch
         X, S, Core = self.X, self.S, self.Core
         if self.step > 0:
