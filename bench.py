@@ -318,7 +318,7 @@ def mixed_bench(n_water=32, thr=1e-5, conver=1e-8, seed=32):
     geom = water_cluster(n_water, seed=seed)
     out = {"workload": f"(H2O){n_water} 6-31G** direct RHF, seed {seed}", "fp32_below": thr, "conver": conver}
     for name, fp in (("fp64", 0.0), ("mixed", thr)):
-        twoe._ctx_cache.clear()
+        twoe.clear_context_cache()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         m = Molecule(geom, "6-31gss")
@@ -487,7 +487,7 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=COMBINED_FP32_B
     from mmd.molecule import Molecule
     E_oracle = plain_mol.polished_energy()
     net = G.network_for(Molecule(geom, "6-31gss"))
-    twoe._ctx_cache.clear()
+    twoe.clear_context_cache()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     m = Molecule(geom, "6-31gss")
@@ -608,7 +608,7 @@ def gpu_arm(args):
     if not args.no_ttc:
         from mmd.integrals import twoe
         for _ in range(TTC_RUNS):
-            twoe._ctx_cache.clear()
+            twoe.clear_context_cache()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             m_ = Molecule(geom, "6-31gss")

@@ -26,6 +26,10 @@
  *                        Molecule.one_electron_integrals (mmd/molecule.py:235-276).
  *   mmdg_boys         <- boys / the _boys test hook (cython/util.pxi:54-55,
  *                        cython/onee.pyx:195-196).
+ *   mmdg_eri_quartets <- ERI(a, b, c, d) (cython/twoe.pyx:36-50) for whole shells:
+ *                        every component of listed shell quartets.
+ *   mmdg_set_partition <- the bra-pair loop of formPT (cython/fock.pyx:38-44) split
+ *                        over GPUs: each rank digests the shell quartets it owns.
  */
 #ifndef MMDG_H
 #define MMDG_H
@@ -89,6 +93,36 @@ int mmdg_set_screen(mmdg_context* ctx, const double* screen, long long n);
 
 /* Full ERI tensor of molecule 0: out is a device array of N^4 doubles (C order). */
 int mmdg_eri_tensor(mmdg_context* ctx, double* out, void* stream);
+
+/*
+ * ERIs of listed shell quartets (the reference's ERI(a, b, c, d) of
+ * cython/twoe.pyx:36-50, applied to every Cartesian component of four shells at once).
+ *   shells   host array of 4n global shell indices (a, b, c, d) in the order of
+ *            mmdg_set_basis; the four shells of a quartet belong to one molecule
+ *   out      device array of n * 1296 doubles: block q holds (ab|cd) at
+ *            out[q*1296 + ((ca*6 + cb)*6 + cc)*6 + cd] for the components ca of a, cb of
+ *            b, ... in the component order of mmdg_set_basis; entries beyond a shell's
+ *            component count are zero
+ * Synchronises `stream` before returning.
+ */
+int mmdg_eri_quartets(mmdg_context* ctx, long long n, const int* shells, double* out, void* stream);
+
+/*
+ * Sharded direct Fock build: the bra-pair loop of formPT (cython/fock.pyx:38-44)
+ * split over `nparts` ranks (one GPU each).  After this call, mmdg_fock and
+ * mmdg_fock_graph of this context digest only the shell quartets of part `part`; the
+ * parts' G add up to the full G (one all-reduce per build).  pair_owner (host,
+ * npairs = the context's shell pairs) gives the owner of every shell pair in
+ * canonical order -- per molecule, s1 ascending, then s2 from the molecule's first
+ * shell to s1 -- and a shell quartet belongs to the owner of its pair with the larger
+ * canonical index s1(s1+1)/2 + s2 (molecule-local shells).  nparts = 1 switches
+ * sharding off (pair_owner may be NULL).
+ */
+int mmdg_set_partition(mmdg_context* ctx, int part, int nparts, const int* pair_owner, long long npairs);
+
+/* Device bytes held by a context (its buffers; the quartet lists once a Fock build
+ * has allocated them).  For caches of contexts; no counterpart in the reference. */
+int mmdg_device_bytes(mmdg_context* ctx, long long* bytes);
 
 /*
  * Direct two-electron Fock update (formPT semantics).
@@ -218,12 +252,15 @@ int mmdg_one_electron(mmdg_context* ctx, int natom, const int* atom_mol, const d
  * static device array of 1,738,240 bytes that every GPU loading the library holds
  * until the process exits.  Limits: 64 shells, 64 functions, 256 primitives, 4096
  * primitive pairs, 131072 E' coefficients, l <= 2; larger inputs fail with
- * MMDG_E_ARG and a message naming the limit.  The first call on a device (the
- * device current) looks up the array's device address and uploads the Boys table;
- * make that first call before any stream capture.  Every call shares the array:
- * calls that overlap on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  The call synchronises `stream` once while staging
- * its inputs.
+ * MMDG_E_ARG and a message naming the limit; so do non-finite exponents,
+ * coefficients or centres.  The first call on a device (the device current) looks
+ * up the array's device address and uploads the Boys table; make that first call
+ * before any stream capture.  Later calls look the address up again and read back a
+ * set-up stamp kept in the array, repeating the set-up when the array is new (after
+ * a cudaDeviceReset).  Every call shares the array: calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialised by the caller; host
+ * threads are serialised inside.  The call synchronises `stream` twice: after
+ * reading the stamp and after staging its inputs.
  */
 int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int* shell_nprim, const double* shell_center,
                             const double* prim_exp, const double* prim_coef, const int* shell_func, int nfunc,

@@ -210,6 +210,8 @@ struct mmdg_context {
   long long nprimpair = 0, nE = 0;
   std::vector<int> pa, pb, pcls, pr_begin, pr_count;
   std::vector<long long> e_off;
+  std::vector<int> pair_row;  // pair index of (s1, s1); (s1, s2 <= s1) is pair_row[s1] + s1 - s2
+  std::vector<int> shell_L, shell_molv;
   DevBuf<int> d_pa, d_pb, d_prb, d_prc;
   DevBuf<long long> d_eoff;
   DevBuf<double4_32a> d_pP;
@@ -235,6 +237,9 @@ struct mmdg_context {
   double* g_G = nullptr;
   double g_tol = -1.0, g_split = -1.0;
   cudaStream_t g_stream = nullptr;
+  // sharded Fock build: owner of every shell pair and its canonical index
+  DevBuf<int> d_pair_owner, d_pair_canon;
+  int part = 0, nparts = 1;
   // screening / Fock scratch
   DevBuf<double> d_screen, d_sq;
   DevBuf<float> d_sqf, d_dPf, d_Dsh;
@@ -535,7 +540,11 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
   h->pr_count.clear();
   h->e_off.clear();
   long long npp = 0, ne = 0;
-  for (int s1 = 0; s1 < nshell; ++s1)
+  h->pair_row.assign(nshell, 0);
+  h->shell_L.assign(shell_L, shell_L + nshell);
+  h->shell_molv.assign(shell_mol, shell_mol + nshell);
+  for (int s1 = 0; s1 < nshell; ++s1) {
+    h->pair_row[s1] = (int)h->pa.size();
     for (int s2 = s1; s2 >= 0 && shell_mol[s2] == shell_mol[s1]; --s2) {
       int a = s1, b = s2;
       if (shell_L[a] < shell_L[b]) std::swap(a, b);
@@ -550,6 +559,7 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
       npp += np;
       ne += (long long)np * nnz_pair(shell_L[a], shell_L[b]);
     }
+  }
   if (npp > 0x7fffffffLL) return fail(MMDG_E_ARG, "mmdg_set_basis: too many primitive pairs");
   h->npair = (int)h->pa.size();
   h->nprimpair = npp;
@@ -821,6 +831,29 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
   return MMDG_OK;
 }
 
+// device bytes held by a context (its buffers, the quartet lists included once a
+// Fock build has allocated them)
+extern "C" int mmdg_device_bytes(mmdg_context* h, long long* bytes) {
+  if (!h || !bytes) return fail(MMDG_E_ARG, "mmdg_device_bytes: null argument");
+  long long b = 0;
+#define MMDG_ADD(buf) b += (long long)(h->buf).n * (long long)sizeof(*(h->buf).p)
+  MMDG_ADD(boys64); MMDG_ADD(boys32);
+  MMDG_ADD(d_center); MMDG_ADD(d_exp); MMDG_ADD(d_coef);
+  MMDG_ADD(d_L); MMDG_ADD(d_nprim); MMDG_ADD(d_poff); MMDG_ADD(d_func); MMDG_ADD(d_shmol); MMDG_ADD(d_shlocal);
+  MMDG_ADD(d_mol_base); MMDG_ADD(d_mol_sbase); MMDG_ADD(d_mol_tbase); MMDG_ADD(d_mol_n); MMDG_ADD(d_mol_ns);
+  MMDG_ADD(d_pa); MMDG_ADD(d_pb); MMDG_ADD(d_prb); MMDG_ADD(d_prc); MMDG_ADD(d_eoff);
+  MMDG_ADD(d_pP); MMDG_ADD(d_pPf); MMDG_ADD(d_E64); MMDG_ADD(d_E32); MMDG_ADD(d_Q);
+  MMDG_ADD(d_mol_shell0); MMDG_ADD(d_screen); MMDG_ADD(d_sq); MMDG_ADD(d_sqf); MMDG_ADD(d_dPf); MMDG_ADD(d_Dsh);
+  MMDG_ADD(d_counters); MMDG_ADD(d_q64); MMDG_ADD(d_q32); MMDG_ADD(d_keyoff); MMDG_ADD(d_qn);
+  MMDG_ADD(d_pair_owner); MMDG_ADD(d_pair_canon);
+  for (int c = 0; c < kNumPairClasses; ++c) {
+    MMDG_ADD(d_cls[c]); MMDG_ADD(d_cls_moff[c]); MMDG_ADD(d_gslot[c]);
+  }
+#undef MMDG_ADD
+  *bytes = b;
+  return MMDG_OK;
+}
+
 extern "C" int mmdg_get_screen(mmdg_context* h, double* screen, long long n) {
   if (!h || !screen) return fail(MMDG_E_ARG, "mmdg_get_screen: null argument");
   if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_get_screen: no basis set");
@@ -847,6 +880,80 @@ extern "C" int mmdg_eri_tensor(mmdg_context* h, double* out, void* stream) {
     ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, 0.f};
     CUDA_TRY(e.tensor(g, t, cl, st));
   }
+  return MMDG_OK;
+}
+
+// ------------------------------------------------------------------ listed shell quartets
+// The caller's quartets (a b|c d) (global shell indices, the four of one molecule)
+// are put in the class table's canonical form -- each pair with its higher-L shell
+// first, the pair of higher class as the bra -- grouped by angular class and
+// evaluated by one thread each; the digest writes every component back in the
+// caller's order.
+extern "C" int mmdg_eri_quartets(mmdg_context* h, long long n, const int* shells, double* out, void* stream) {
+  if (!h || (n > 0 && (!shells || !out))) return fail(MMDG_E_ARG, "mmdg_eri_quartets: null argument");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_eri_quartets: no basis set");
+  if (n < 0 || n > 0x7fffffffLL / kQuartetBlock) return fail(MMDG_E_ARG, "mmdg_eri_quartets: bad quartet count");
+  if (n == 0) return MMDG_OK;
+  DeviceGuard dgd(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<std::vector<QuartetItem>> per(MMDG_NCLASS);
+  int class_index[kNumPairClasses][kNumPairClasses];
+  for (int x = 0; x < kNumPairClasses; ++x)
+    for (int y = 0; y < kNumPairClasses; ++y) class_index[x][y] = -1;
+  {
+    int ci = 0;
+    for (const ClassEntry& e : kClasses) class_index[pair_class(e.la, e.lb)][pair_class(e.lc, e.ld)] = ci++;
+  }
+  // canonical pair of shells (x, y): its index and whether y is the stored first shell
+  auto pair_of = [&](int x, int y, int* flip) {
+    const int s1 = std::max(x, y), s2 = std::min(x, y);
+    const int p = h->pair_row[s1] + (s1 - s2);
+    *flip = (h->pa[p] != x) ? 1 : 0;
+    return p;
+  };
+  for (long long q = 0; q < n; ++q) {
+    const int* sq = shells + 4 * q;
+    for (int k = 0; k < 4; ++k)
+      if (sq[k] < 0 || sq[k] >= h->nshell) return fail(MMDG_E_ARG, "mmdg_eri_quartets: shell index out of range");
+    const int m = h->shell_molv[sq[0]];
+    if (h->shell_molv[sq[1]] != m || h->shell_molv[sq[2]] != m || h->shell_molv[sq[3]] != m)
+      return fail(MMDG_E_ARG, "mmdg_eri_quartets: the four shells of a quartet must belong to one molecule");
+    int f1 = 0, f2 = 0;
+    const int p1 = pair_of(sq[0], sq[1], &f1), p2 = pair_of(sq[2], sq[3], &f2);
+    const int c1 = h->pcls[p1], c2 = h->pcls[p2];
+    QuartetItem it;
+    it.slot = (int)q;
+    if (c1 >= c2) {
+      it.bra = p1;
+      it.ket = p2;
+      it.flags = (f1 ? 2 : 0) | (f2 ? 4 : 0);
+    } else {
+      it.bra = p2;
+      it.ket = p1;
+      it.flags = 1 | (f1 ? 2 : 0) | (f2 ? 4 : 0);
+    }
+    per[class_index[h->pcls[it.bra]][h->pcls[it.ket]]].push_back(it);
+  }
+  std::vector<QuartetItem> all;
+  std::vector<size_t> beg(MMDG_NCLASS + 1, 0);
+  for (int c = 0; c < MMDG_NCLASS; ++c) {
+    beg[c] = all.size();
+    all.insert(all.end(), per[c].begin(), per[c].end());
+  }
+  beg[MMDG_NCLASS] = all.size();
+  DevBuf<QuartetItem> d_items;
+  if (d_items.alloc(all.size()) != cudaSuccess) return fail(MMDG_E_NOMEM, "mmdg_eri_quartets: allocation");
+  CUDA_TRY(cudaMemcpyAsync(d_items.p, all.data(), sizeof(QuartetItem) * all.size(), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double) * (size_t)n * kQuartetBlock, st));
+  Geometry g = h->geom();
+  QuartetArgs qa{out};
+  int ci = 0;
+  for (const ClassEntry& e : kClasses) {
+    const int cnt = (int)(beg[ci + 1] - beg[ci]);
+    if (cnt) CUDA_TRY(e.quartets(g, qa, d_items.p + beg[ci], cnt, st));
+    ++ci;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));  // the item list is released on return
   return MMDG_OK;
 }
 
@@ -933,6 +1040,10 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   f.tol = tol;
   f.tolf_lo = float(tol * (1.0 - 1e-4));
   f.tolf_hi = float(tol * (1.0 + 1e-4));
+  f.counters = nullptr;
+  f.pair_owner = h->nparts > 1 ? h->d_pair_owner.p : nullptr;
+  f.pair_canon = h->d_pair_canon.p;
+  f.part = h->part;
   const float split = float(fp32_below);
   // ---- quartet-list storage (first use): per class, buckets (bra group, ket group)
   if (h->q_off.empty()) {
@@ -1589,6 +1700,48 @@ extern "C" int mmdg_set_streams(mmdg_context* h, int nstreams) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
+  return MMDG_OK;
+}
+
+// Sharded Fock build: later builds of this context digest only the shell quartets of
+// part `part` of `nparts`.  pair_owner[k] (host, 0..nparts-1) is the owner of the k-th
+// shell pair in canonical order -- for each molecule, s1 ascending, then s2 = first
+// shell of the molecule .. s1 (global shell indices), i.e. by s1(s1+1)/2 + s2 -- and a
+// shell quartet belongs to the owner of its pair with the larger canonical index, so
+// the parts' G add up to the full G.  nparts = 1 (pair_owner may be null) switches
+// sharding off.
+extern "C" int mmdg_set_partition(mmdg_context* h, int part, int nparts, const int* pair_owner, long long npairs) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_partition: null context");
+  if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_set_partition: no basis set");
+  if (nparts < 1 || part < 0 || part >= nparts) return fail(MMDG_E_ARG, "mmdg_set_partition: bad part / nparts");
+  DeviceGuard dgd(h->device);
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  if (nparts == 1) {
+    h->part = 0;
+    h->nparts = 1;
+    return MMDG_OK;
+  }
+  if (!pair_owner || npairs != h->npair) return fail(MMDG_E_ARG, "mmdg_set_partition: one owner per shell pair");
+  std::vector<int> own(h->npair), canon(h->npair);
+  long long k = 0;
+  for (int s1 = 0; s1 < h->nshell; ++s1) {
+    int first = s1;
+    while (first > 0 && h->shell_molv[first - 1] == h->shell_molv[s1]) --first;
+    for (int s2 = first; s2 <= s1; ++s2, ++k) {
+      const int o = pair_owner[k];
+      if (o < 0 || o >= nparts) return fail(MMDG_E_ARG, "mmdg_set_partition: owner out of range");
+      const int p = h->pair_row[s1] + (s1 - s2);
+      own[p] = o;
+      canon[p] = (s1 - first) * (s1 - first + 1) / 2 + (s2 - first);
+    }
+  }
+  if (h->d_pair_owner.upload(own) != cudaSuccess || h->d_pair_canon.upload(canon) != cudaSuccess)
+    return fail(MMDG_E_NOMEM, "mmdg_set_partition: allocation");
+  h->part = part;
+  h->nparts = nparts;
   return MMDG_OK;
 }
 

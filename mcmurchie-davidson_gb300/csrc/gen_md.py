@@ -365,20 +365,22 @@ def generate_instances(outdir, ngroups=6):
             "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
-            "struct ClassEntry { int la, lb, lc, ld; fock_fn fock; tensor_fn tensor; schwarz_fn schwarz; };"]
+            "typedef cudaError_t (*quartets_fn)(const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);",
+            "struct ClassEntry { int la, lb, lc, ld; fock_fn fock; tensor_fn tensor; schwarz_fn schwarz; quartets_fn quartets; };"]
     for g in range(ngroups):
         decl.append(f"cudaError_t init_group{g}();")
     for c in cls:
         s = "".join(map(str, c))
         decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);")
         decl.append(f"cudaError_t launch_tensor_{s}(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);")
+        decl.append(f"cudaError_t launch_quartets_{s}(const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);")
         if c[:2] == c[2:]:
             decl.append(f"cudaError_t launch_schwarz_{s}(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);")
     decl.append("static const ClassEntry kClasses[] = {")
     for c in cls:
         s = "".join(map(str, c))
         sch = f"launch_schwarz_{s}" if c[:2] == c[2:] else "nullptr"
-        decl.append(f"  {{{c[0]}, {c[1]}, {c[2]}, {c[3]}, launch_fock_{s}, launch_tensor_{s}, {sch}}},")
+        decl.append(f"  {{{c[0]}, {c[1]}, {c[2]}, {c[3]}, launch_fock_{s}, launch_tensor_{s}, {sch}, launch_quartets_{s}}},")
     decl.append("};")
     decl.append(f"static const int kNumGroups = {ngroups};")
     decl.append("static cudaError_t (*const kGroupInit[])() = {" + ", ".join(f"init_group{g}" for g in range(ngroups)) + "};")
@@ -400,6 +402,11 @@ def generate_instances(outdir, ngroups=6):
             t.append(f"  k_tensor<{md}<double>><<<grid, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, cl);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
+            t.append(f"cudaError_t launch_quartets_{s}(const Geometry& g, const QuartetArgs& a, const QuartetItem* items, int n, cudaStream_t st) {{")
+            t.append(f"  k_quartets<{md}<double>><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, items, n);")
+            t.append(f"  return cudaGetLastError();")
+            t.append("}")
+            inits.append(f"  if ((e = cudaFuncSetAttribute(k_quartets<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<double>, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<float>, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<float>, float>()))) return e;")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_tensor<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")

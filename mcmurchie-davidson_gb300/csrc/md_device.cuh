@@ -289,6 +289,11 @@ struct FockArgs {
   double tol;
   float tolf_lo, tolf_hi;  // FP32 guard band around tol
   unsigned long long* counters;  // [0] computed function quartets, [1] computed shell quartets
+  // sharded build (mmdg_set_partition): a shell quartet is kept only if the owner of
+  // its pair with the larger canonical index is `part` (pair_owner null: no sharding)
+  const int* pair_owner;  // per shell pair
+  const int* pair_canon;  // canonical index s1(s1+1)/2 + s2 of every shell pair (per molecule)
+  int part;
 };
 
 template <int NB, int ND>
@@ -400,6 +405,49 @@ struct TensorDigest {
     o[((l * N + k) * N + i) * N + j] = v;
     o[((i * N + j) * N + l) * N + k] = v;
     o[((k * N + l) * N + j) * N + i] = v;
+  }
+};
+
+// Listed shell quartets (mmdg_eri_quartets; the reference's ERI(a, b, c, d),
+// twoe.pyx:36-50, on whole shells): every component of the caller's (ab|cd) in the
+// caller's shell order, at out[q*1296 + ((ca*6+cb)*6+cc)*6+cd] -----------------------
+constexpr int kQuartetBlock = kMaxComp * kMaxComp * kMaxComp * kMaxComp;
+
+struct QuartetArgs {
+  double* out;  // n * kQuartetBlock
+};
+
+// one listed quartet: canonical bra / ket shell pair, output slot, orientation flags
+//   bit 0: the caller's first pair is the canonical ket
+//   bit 1: the caller's first pair lists the canonical second shell first
+//   bit 2: the same for the caller's second pair
+struct QuartetItem {
+  int bra, ket, slot, flags;
+};
+
+template <int NB, int ND>
+struct QuartetDigest {
+  const QuartetArgs& a;
+  long long base;
+  int flags;
+  __device__ __forceinline__ QuartetDigest(const QuartetArgs& a_, int slot, int flags_)
+      : a(a_), base((long long)slot * kQuartetBlock), flags(flags_) {}
+  template <typename Real>
+  __device__ __forceinline__ void put(int ca, int cb, int cc, int cd, Real vr) {
+    int b0 = ca, b1 = cb, k0 = cc, k1 = cd;
+    int u0, u1, u2, u3;
+    if (flags & 1) {
+      u0 = (flags & 2) ? k1 : k0;
+      u1 = (flags & 2) ? k0 : k1;
+      u2 = (flags & 4) ? b1 : b0;
+      u3 = (flags & 4) ? b0 : b1;
+    } else {
+      u0 = (flags & 2) ? b1 : b0;
+      u1 = (flags & 2) ? b0 : b1;
+      u2 = (flags & 4) ? k1 : k0;
+      u3 = (flags & 4) ? k0 : k1;
+    }
+    a.out[base + ((u0 * kMaxComp + u1) * kMaxComp + u2) * kMaxComp + u3] = double(vr);
   }
 };
 

@@ -1,10 +1,14 @@
 // md_kernels.cuh -- the shell-quartet kernels (one instantiation per angular class).
 //
-// One thread evaluates one contracted shell quartet (ab|cd) of a class list pair:
-//   blockIdx.x        -> bra shell pair (slot in the bra class list)
-//   blockIdx.y*128+tx -> ket shell pair (slot in the ket class list)
-// Class lists are sorted by (primitive count, Schwarz bound descending), so a warp's
-// 32 kets share their primitive loop trip counts and their screening outcome.
+// Fock builds (formPT semantics) run in two launches per angular class: k_screen
+// walks every candidate (bra shell pair, ket shell pair) of the class and appends
+// the survivors of the Schwarz x density bound to bucketed quartet lists (buckets
+// keyed by the primitive-count groups of the two pairs, FP64 and FP32 lists); then
+// k_fock, a persistent grid-stride kernel, evaluates the list, one thread per
+// (quartet, ket chunk), chunk-major, so a warp shares its code path and, inside a
+// bucket, its primitive trip counts.  The compact high-L classes have a
+// warp-cooperative Fock kernel of their own (md_warp.cuh).  The ERI tensor, the
+// Schwarz table and listed quartets use one thread per shell quartet.
 #pragma once
 #include "md_device.cuh"
 #include "md_gen.cuh"
@@ -105,6 +109,11 @@ static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs
                              fmaxf(fmaxf(__ldg(D + a * S + c), __ldg(D + a * S + d)),
                                    fmaxf(__ldg(D + b * S + c), __ldg(D + b * S + d))));
       keep = qq * dm >= f.tolf_lo;
+      if (f.pair_owner) {
+        const int own = __ldg(f.pair_canon + bp) >= __ldg(f.pair_canon + kp) ? __ldg(f.pair_owner + bp)
+                                                                              : __ldg(f.pair_owner + kp);
+        keep = keep && own == f.part;
+      }
       key = gb * ql.nkg + __ldg(ql.gket + jk);
     }
     const bool lo = qq < cl.qmax;  // qmax carries the FP32 split (0: none)
@@ -187,6 +196,19 @@ __global__ void __launch_bounds__(kThreads) k_tensor(Geometry g, TensorArgs t, C
   Ctx<double> c = make_ctx<MD, double>(g, bp, kp, rs);
   QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, mol};
   TensorDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, t, q);
+  MD::run(c, dg);
+}
+
+// listed shell quartets of one class (mmdg_eri_quartets): one thread per item
+template <class MD>
+__global__ void __launch_bounds__(kThreads) k_quartets(Geometry g, QuartetArgs a, const QuartetItem* items, int n) {
+  const int idx = blockIdx.x * kThreads + threadIdx.x;
+  if (idx >= n) return;
+  const QuartetItem it = items[idx];
+  extern __shared__ double smem_d[];
+  double* rs = smem_d + threadIdx.x;
+  Ctx<double> c = make_ctx<MD, double>(g, it.bra, it.ket, rs);
+  QuartetDigest<ncart(MD::LB), ncart(MD::LD)> dg(a, it.slot, it.flags);
   MD::run(c, dg);
 }
 

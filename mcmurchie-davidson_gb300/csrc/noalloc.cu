@@ -13,13 +13,18 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress -- in host code the symbol name
 // is only a host-side stand-in -- and uploads the Boys table into it.  That first
-// call should come before any stream capture.  All calls share the array and it
-// keeps the previous call's contents: everything a call reads is rewritten by the
-// same call before use, and the output tensor is cleared.  Calls that overlap on
-// the GPU (different streams, or several host threads) race on the array; callers
-// must serialise them.
+// call should come before any stream capture.  Every later call looks the address
+// up again (cheap, no allocation) and repeats the set-up if it changed, as after a
+// cudaDeviceReset, which reloads the module with a fresh array.  All calls share
+// the array and it keeps the previous call's contents: everything a call reads is
+// rewritten by the same call before use, and the output tensor is cleared.  Calls
+// that overlap on the GPU (different streams, or several host threads) race on the
+// array; callers must serialise them.  The host-side bookkeeping lives in static
+// arrays under one mutex (no heap, and about 1 KB of stack), so host threads are
+// serialised here.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -54,6 +59,8 @@ constexpr int kIntPair = kNA_MaxPair * 4;
 constexpr int kIntLists = kNA_MaxPair;
 constexpr size_t kOffEoff = al(kOffInts + sizeof(int) * (kIntShell + kIntPair + kIntLists + 8));
 constexpr size_t kOffMol = al(kOffEoff + sizeof(long long) * kNA_MaxPair);
+constexpr size_t kOffStamp = kOffMol + 48;  // 8 bytes, inside the molecule slot's spare tail
+constexpr unsigned long long kNAStamp = 0x4d4d4447'4e413031ULL;
 constexpr size_t kNoAllocScratchBytes = al(kOffMol + 64);
 
 }  // namespace
@@ -67,6 +74,18 @@ std::mutex g_na_mutex;
 void* g_na_base[64] = {};        // device address of g_noalloc_scratch per device
 double g_na_boys[kBoysTabSize];  // host copy of the Boys table (static storage)
 bool g_na_boys_ready = false;
+
+// host staging of one call (static storage, used under g_na_mutex only)
+struct NaHost {
+  int L[kNA_MaxShell], K[kNA_MaxShell], poff[kNA_MaxShell], shlocal[kNA_MaxShell], shmol[kNA_MaxShell];
+  int pa[kNA_MaxPair], pb[kNA_MaxPair], prb[kNA_MaxPair], prc[kNA_MaxPair], pcls[kNA_MaxPair];
+  long long eoff[kNA_MaxPair];
+  int lists[kNA_MaxPair], lbeg[kNA_PairClasses + 1];
+  int ints[kIntShell + kIntPair + kIntLists + 8];
+  long long mol[4];
+  int moln[2];
+};
+NaHost g_na_host;
 int na_fail(int code, const char* msg) { return mmdg_internal_fail(code, msg); }
 
 int nnz_pair_na(int la, int lb) {
@@ -94,8 +113,14 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: more than 64 shells (scratch limit)");
   if (nfunc > kNA_MaxFunc)
     return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: more than 64 basis functions (scratch limit)");
-  // ---------------- host bookkeeping in fixed-size arrays
-  int L[kNA_MaxShell], K[kNA_MaxShell], poff[kNA_MaxShell], shlocal[kNA_MaxShell], shmol[kNA_MaxShell];
+  // ---------------- host bookkeeping in the static staging arrays
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  NaHost& H = g_na_host;
+  int* L = H.L;
+  int* K = H.K;
+  int* poff = H.poff;
+  int* shlocal = H.shlocal;
+  int* shmol = H.shmol;
   int total_prim = 0;
   for (int s = 0; s < nshell; ++s) {
     if (shell_L[s] < 0) return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: negative angular momentum");
@@ -118,9 +143,16 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     }
   }
   for (int p = 0; p < total_prim; ++p)
-    if (!(prim_exp[p] > 0.0)) return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: exponents must be positive");
-  int pa[kNA_MaxPair], pb[kNA_MaxPair], prb[kNA_MaxPair], prc[kNA_MaxPair], pcls[kNA_MaxPair];
-  long long eoff[kNA_MaxPair];
+    if (!(prim_exp[p] > 0.0) || !std::isfinite(prim_exp[p]) || !std::isfinite(prim_coef[p]))
+      return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: exponents must be positive and finite");
+  for (int x = 0; x < 3 * nshell; ++x)
+    if (!std::isfinite(shell_center[x])) return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: non-finite centre");
+  int* pa = H.pa;
+  int* pb = H.pb;
+  int* prb = H.prb;
+  int* prc = H.prc;
+  int* pcls = H.pcls;
+  long long* eoff = H.eoff;
   int npair = 0;
   long long npp = 0, ne = 0;
   for (int s1 = 0; s1 < nshell; ++s1)
@@ -145,7 +177,8 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: more than 4096 primitive pairs (scratch limit)");
   if (ne > kNA_MaxE) return na_fail(MMDG_E_ARG, "mmdg_eri_tensor_noalloc: E' tables exceed the scratch limit");
   // class lists, concatenated
-  int lists[kNA_MaxPair], lbeg[kNA_PairClasses + 1];
+  int* lists = H.lists;
+  int* lbeg = H.lbeg;
   {
     int n = 0;
     for (int c = 0; c < kNA_PairClasses; ++c) {
@@ -155,8 +188,8 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     }
     lbeg[kNA_PairClasses] = n;
   }
-  std::lock_guard<std::mutex> lock(g_na_mutex);
-  // ---------------- set-up, once per device: device address of the scratch, Boys table
+  // ---------------- set-up per device: device address of the scratch, Boys table;
+  // the address is looked up on every call and the set-up repeated when it changed
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 64) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: no device");
@@ -164,10 +197,18 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     mmdg_fill_boys_table(g_na_boys);
     g_na_boys_ready = true;
   }
-  if (!g_na_base[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: cudaGetSymbolAddress failed");
+  void* ptr = nullptr;
+  e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: cudaGetSymbolAddress failed");
+  cudaStream_t st = (cudaStream_t)stream;
+  // a stamp written at set-up tells an initialised array from a fresh (zeroed) one,
+  // e.g. after cudaDeviceReset reloaded the module at the same address
+  unsigned long long stamp = 0;
+  e = cudaMemcpyAsync(&stamp, static_cast<char*>(ptr) + kOffStamp, sizeof(stamp), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: reading the set-up stamp failed");
+  if (g_na_base[dev] != ptr || stamp != kNAStamp) {
+    g_na_base[dev] = nullptr;
     e = cudaMemcpy(static_cast<char*>(ptr) + kOffBoys, g_na_boys, sizeof(double) * kBoysTabSize,
                    cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: Boys table upload failed");
@@ -175,12 +216,14 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     for (int gi = 0; gi < kNumGroups; ++gi)
       if (kGroupInit[gi]() != cudaSuccess)
         return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: kernel attribute set-up failed");
+    static const unsigned long long kStampValue = kNAStamp;
+    e = cudaMemcpy(static_cast<char*>(ptr) + kOffStamp, &kStampValue, sizeof(kStampValue), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return na_fail(MMDG_E_CUDA, "mmdg_eri_tensor_noalloc: writing the set-up stamp failed");
     g_na_base[dev] = ptr;
   }
   char* base = static_cast<char*>(g_na_base[dev]);
-  cudaStream_t st = (cudaStream_t)stream;
   // ---------------- stage inputs into the scratch (stream ordered)
-  int ints[kIntShell + kIntPair + kIntLists + 8];
+  int* ints = H.ints;
   int* iL = ints;
   int* iK = iL + kNA_MaxShell;
   int* iP = iK + kNA_MaxShell;
@@ -207,8 +250,13 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
     iprc[p] = prc[p];
   }
   for (int p = 0; p < npair; ++p) ilist[p] = lists[p];
-  long long mol[4] = {0, (long long)nfunc, 0, 0};  // mol_base, mol_n (as int below)
-  int moln[2] = {nfunc, nshell};
+  long long* mol = H.mol;  // mol_base (mol_n as int below)
+  mol[0] = 0;
+  mol[1] = nfunc;
+  mol[2] = mol[3] = 0;
+  int* moln = H.moln;
+  moln[0] = nfunc;
+  moln[1] = nshell;
   double* dCenter = reinterpret_cast<double*>(base + kOffCenter);
   double* dExp = reinterpret_cast<double*>(base + kOffExp);
   double* dCoef = reinterpret_cast<double*>(base + kOffCoef);
@@ -223,11 +271,12 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
   NA_TRY(cudaMemcpyAsync(dCenter, shell_center, sizeof(double) * 3 * nshell, cudaMemcpyHostToDevice, st));
   NA_TRY(cudaMemcpyAsync(dExp, prim_exp, sizeof(double) * total_prim, cudaMemcpyHostToDevice, st));
   NA_TRY(cudaMemcpyAsync(dCoef, prim_coef, sizeof(double) * total_prim, cudaMemcpyHostToDevice, st));
-  NA_TRY(cudaMemcpyAsync(dInts, ints, sizeof(ints), cudaMemcpyHostToDevice, st));
+  NA_TRY(cudaMemcpyAsync(dInts, ints, sizeof(H.ints), cudaMemcpyHostToDevice, st));
   NA_TRY(cudaMemcpyAsync(dEoff, eoff, sizeof(long long) * npair, cudaMemcpyHostToDevice, st));
   NA_TRY(cudaMemcpyAsync(dMolBase, mol, sizeof(long long), cudaMemcpyHostToDevice, st));
   NA_TRY(cudaMemcpyAsync(dMolN, moln, sizeof(int), cudaMemcpyHostToDevice, st));
-  // pageable sources: make sure the copies have consumed the stack arrays
+  // pageable sources: make sure the copies have consumed the staging arrays before
+  // the next call (or another thread, after the mutex) rewrites them
   NA_TRY(cudaStreamSynchronize(st));
   // ---------------- primitive pairs
   double4_32a* dPP = reinterpret_cast<double4_32a*>(base + kOffPP);

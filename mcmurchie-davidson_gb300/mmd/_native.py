@@ -49,6 +49,9 @@ def _bind(L):
         "mmdg_set_prim_tol": (c_int, [p, ctypes.c_double]),
         "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, c_d, p, p]),
         "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),
+        "mmdg_eri_quartets": (c_int, [p, c_ll, p, p, p]),
+        "mmdg_set_partition": (c_int, [p, c_int, c_int, p, c_ll]),
+        "mmdg_device_bytes": (c_int, [p, ctypes.POINTER(c_ll)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -133,7 +136,7 @@ class Context:
         self.base = np.concatenate([[0], np.cumsum(self.nfunc.astype(np.int64) ** 2)[:-1]])
         self.tbase = np.concatenate([[0], np.cumsum(self.nfunc.astype(np.int64) * (self.nfunc + 1) // 2)[:-1]])
         self.last_counts = None
-        self._user_screen = None
+        self.nparts = 1  # sharded Fock builds (set_partition)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -168,6 +171,60 @@ class Context:
             out = torch.empty((N, N, N, N), dtype=torch.float64, device=f"cuda:{self.device}")
         check(lib().mmdg_eri_tensor(self._h, ctypes.c_void_p(out.data_ptr()), stream_ptr()), "mmdg_eri_tensor")
         return out
+
+    def eri_quartets(self, shells, out=None):
+        """All component ERIs of listed shell quartets: ``shells`` is an (n, 4) array of
+        global shell indices (a, b, c, d); returns a device tensor (n, 6, 6, 6, 6) with
+        (ab|cd) for components [ca, cb, cc, cd] in the caller's shell order (entries
+        beyond a shell's components are zero)."""
+        torch = self.torch
+        q = np.ascontiguousarray(shells, dtype=np.int32).reshape(-1, 4)
+        n = q.shape[0]
+        if out is None:
+            out = torch.empty((n, MAX_COMP, MAX_COMP, MAX_COMP, MAX_COMP), dtype=torch.float64,
+                              device=f"cuda:{self.device}")
+        check(lib().mmdg_eri_quartets(self._h, n, _ptr(q), ctypes.c_void_p(out.data_ptr()), stream_ptr()),
+              "mmdg_eri_quartets")
+        return out
+
+    def function_quartets(self, idx, mol: int = 0):
+        """ERIs (ij|kl) of listed function quartets of molecule ``mol`` (an (n, 4) array
+        of molecule-local function indices), as a host array of n values."""
+        idx = np.asarray(idx, dtype=np.int64).reshape(-1, 4)
+        ss = self.sets[mol]
+        base = sum(s.nshell for s in self.sets[:mol])
+        fshell = np.full(ss.nfunc, -1, dtype=np.int64)
+        fcomp = np.zeros(ss.nfunc, dtype=np.int64)
+        for s, row in enumerate(ss.func):
+            for c, f in enumerate(row):
+                if f >= 0:
+                    fshell[f], fcomp[f] = s, c
+        sh = fshell[idx]
+        uq, inv = np.unique(sh, axis=0, return_inverse=True)
+        blocks = self.eri_quartets(uq + base).cpu().numpy()
+        inv = inv.reshape(-1)
+        c = fcomp[idx]
+        return blocks[inv, c[:, 0], c[:, 1], c[:, 2], c[:, 3]]
+
+    def set_partition(self, part: int, nparts: int, owner=None):
+        """Shard later Fock builds: only the shell quartets of ``part`` (owner per
+        canonical shell pair, ``mmd.distributed.canonical_pairs`` order); nparts = 1
+        switches sharding off."""
+        if int(nparts) == 1:
+            check(lib().mmdg_set_partition(self._h, 0, 1, None, 0), "mmdg_set_partition")
+            self.nparts = 1
+            return
+        o = np.ascontiguousarray(owner, dtype=np.int32)
+        check(lib().mmdg_set_partition(self._h, int(part), int(nparts), _ptr(o), o.size), "mmdg_set_partition")
+        self.nparts = int(nparts)
+
+    def device_bytes(self) -> int:
+        """Device memory held by this context (quartet lists included once allocated)."""
+        if not getattr(self, "_h", None):
+            return 0
+        b = ctypes.c_longlong()
+        check(lib().mmdg_device_bytes(self._h, ctypes.byref(b)), "mmdg_device_bytes")
+        return int(b.value)
 
     def fock(self, dP, G=None, tol: float = 1e-12, fp32_below: float = 0.0, counts: bool = False):
         """Unsymmetrised G(dP) (formPT semantics); dP/G are packed device float64 tensors."""

@@ -285,7 +285,10 @@ class BatchRHF:
                     # converged (frozen) molecules: a well-posed dummy system
                     eye = torch.eye(n + 1, dtype=torch.float64, device=self.dev).expand(B, -1, -1)
                     Bm = torch.where(active, Bm, eye)
-                    w = torch.linalg.solve(Bm, rhs)
+                    # the B small (n+1)^2 systems are solved on the host (LAPACK), like the
+                    # eigensolves: no dependence on torch's CUDA linear-algebra library
+                    w = torch.as_tensor(np.linalg.solve(Bm.cpu().numpy(), rhs.cpu().numpy()[..., None])[..., 0],
+                                        device=self.dev)
                     Fd = torch.einsum("bi,bijk->bjk", w[:, :n], torch.stack(hist_F, 1))
                     FO = X.transpose(1, 2) @ Fd @ X
                     if revert is not None:  # restart from the core guess: F = Core, P_old = 0

@@ -13,22 +13,46 @@ from .twoe import context_for
 
 
 def _screen_array(screen, N):
-    if isinstance(screen, dict):
-        return np.fromiter((screen[i] for i in range(N * (N + 1) // 2)), dtype=np.float64, count=N * (N + 1) // 2)
-    return np.ascontiguousarray(screen, dtype=np.float64)
+    """The Schwarz table as a flat array screen[p(p+1)/2+q], read at call time like the
+    reference's per-quartet ``screen[ij]`` lookups (fock.pyx:46-48), so values edited
+    in place are seen.  A dict whose keys are 0..n-1 in insertion order (how
+    ``Molecule.build`` makes it) is read through ``values()``; its key order is
+    verified once per dict object and length, any other dict key by key."""
+    n = N * (N + 1) // 2
+    if not isinstance(screen, dict):
+        return np.ascontiguousarray(screen, dtype=np.float64).reshape(-1)
+    if len(screen) == n:
+        memo = _KEY_ORDER_OK.get(id(screen))
+        if memo is None or memo[0] is not screen or memo[1] != n:
+            ok = next(iter(screen)) == 0 and next(reversed(screen)) == n - 1 and \
+                all(a == b for a, b in zip(screen, range(n)))
+            memo = (screen, n, ok)
+            _KEY_ORDER_OK.clear()  # one dict remembered at a time
+            _KEY_ORDER_OK[id(screen)] = memo
+        if memo[2] and next(reversed(screen)) == n - 1:
+            return np.fromiter(screen.values(), dtype=np.float64, count=n)
+    return np.fromiter(map(screen.__getitem__, range(n)), dtype=np.float64, count=n)
+
+
+_KEY_ORDER_OK: dict = {}
 
 
 def formPT(P, P_old, bfs, nbasis, screen, tol):
     """Two-electron Fock contribution G(P - P_old), unsymmetrised, as a complex N x N
     array (cython/fock.pyx:13-87): the reference's Schwarz x density screening of
     every function quartet at ``tol``, degeneracy factors and scatter, computed by
-    the GPU class kernels (a complex density difference is two real builds)."""
+    the GPU class kernels (a complex density difference is two real builds).  The
+    Schwarz table is re-uploaded to the device whenever its contents differ from
+    the last upload (``screen=None`` keeps the table the device computed)."""
     N = int(nbasis)
     ctx = context_for(bfs)
     torch = ctx.torch
-    if screen is not None and screen is not getattr(ctx, "_user_screen_obj", None):
-        ctx.set_screen(_screen_array(screen, N))
-        ctx._user_screen_obj = screen
+    if screen is not None:
+        arr = _screen_array(screen, N)
+        last = getattr(ctx, "_user_screen_arr", None)
+        if last is None or last.shape != arr.shape or not np.array_equal(last, arr):
+            ctx.set_screen(arr)
+            ctx._user_screen_arr = arr
     dP = np.asarray(P) - np.asarray(P_old)
     parts = [np.real(dP)]
     if np.iscomplexobj(dP) and np.any(np.imag(dP) != 0):

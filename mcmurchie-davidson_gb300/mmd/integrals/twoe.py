@@ -7,6 +7,9 @@ CPU path.
 """
 from __future__ import annotations
 
+import os
+from collections import OrderedDict
+
 import numpy as np
 
 from .. import _native
@@ -63,7 +66,32 @@ class Basis:
         return self.norm
 
 
-_ctx_cache: dict = {}
+# Device contexts by basis fingerprint, least recently used first.  The cache is
+# bounded by the device bytes its contexts hold (a context's quartet lists grow as
+# S^4/8 in the number of shells: 1.4 GB for (H2O)16 6-31G**, 22 GB for (H2O)32) and
+# by a count; the oldest contexts are released first.  MMD_CONTEXT_CACHE_BYTES
+# overrides the byte budget.
+_ctx_cache: "OrderedDict" = OrderedDict()
+CONTEXT_CACHE_MAX = 16
+CONTEXT_CACHE_BYTES = int(float(os.environ.get("MMD_CONTEXT_CACHE_BYTES", 48e9)))
+
+
+def _trim_cache(keep=None):
+    total = 0
+    sizes = {}
+    for k, c in _ctx_cache.items():
+        sizes[k] = c.device_bytes()
+        total += sizes[k]
+    while _ctx_cache and (len(_ctx_cache) > CONTEXT_CACHE_MAX or total > CONTEXT_CACHE_BYTES):
+        k = next(iter(_ctx_cache))
+        if k == keep:
+            if len(_ctx_cache) == 1:
+                break
+            _ctx_cache.move_to_end(k)
+            continue
+        c = _ctx_cache.pop(k)
+        total -= sizes.pop(k)
+        c.close()
 
 
 def context_for(bfs):
@@ -71,20 +99,27 @@ def context_for(bfs):
     key = fingerprint(bfs)
     ctx = _ctx_cache.get(key)
     if ctx is None:
-        if len(_ctx_cache) > 8:
-            _ctx_cache.clear()
         ctx = _native.Context(shells_from_bfs(bfs))
         _ctx_cache[key] = ctx
+        _trim_cache(keep=key)
+    else:
+        _ctx_cache.move_to_end(key)
     return ctx
 
 
+def clear_context_cache():
+    """Release every cached device context."""
+    while _ctx_cache:
+        _ctx_cache.popitem(last=False)[1].close()
+
+
 def ERI(a, b, c, d) -> float:
-    """Contracted ERI (ab|cd) of four basis functions (twoe.pyx:36-50)."""
-    ctx = _native.Context(shells_from_bfs([a, b, c, d]))
-    T = ctx.eri_tensor()
-    v = float(T[0, 1, 2, 3].item())
-    ctx.close()
-    return v
+    """Contracted ERI (ab|cd) of four basis functions (twoe.pyx:36-50): one shell
+    quartet evaluated by the class kernels (``mmdg_eri_quartets``) in the cached
+    context of the four functions."""
+    ctx = context_for([a, b, c, d])
+    v = ctx.function_quartets(np.array([[0, 1, 2, 3]], dtype=np.int32))
+    return float(v[0])
 
 
 def doERIs(N, TwoE, bfs):

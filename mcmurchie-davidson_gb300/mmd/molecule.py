@@ -253,15 +253,15 @@ class Molecule(SCF, Forces):
         for pair in itertools.combinations(self.atoms, 2):
             self.nuc_energy += pair[0].charge * pair[1].charge / np.linalg.norm(pair[0].origin - pair[1].origin)
         self.Core = self.T + self.V
-        # S^{-1/2} and S^{1/2} by the symmetric eigendecomposition (on the device)
-        Sd = self._dev["S"]
-        w, U = torch.linalg.eigh(Sd)
-        Xd = (U * w.rsqrt()) @ U.T
-        Ud = (U * w.sqrt()) @ U.T
-        self._dev["X"] = Xd
+        # S^{-1/2} and S^{1/2} by the symmetric eigendecomposition of S on the host cores
+        # (LAPACK dsyevd, the SCF's own eigensolver up to ~1000 functions): one solve per
+        # basis, and no dependence on torch's CUDA linear-algebra library
+        from .scf import host_eigh
+        w, U = host_eigh(self.S)
+        self.X = (U * (1.0 / np.sqrt(w))) @ U.T
+        self.U = (U * np.sqrt(w)) @ U.T
+        self._dev["X"] = torch.as_tensor(self.X, device=dev)
         self._dev["Core"] = self._dev["T"] + self._dev["V"]
-        self.X = Xd.cpu().numpy()
-        self.U = Ud.cpu().numpy()
 
     def two_electron_integrals(self):
         """Full ERI tensor on the GPU (molecule.py:288-293)."""

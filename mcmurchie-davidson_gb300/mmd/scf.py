@@ -10,9 +10,11 @@ reference's algorithm step for step (mmd/scf.py:10-80):
 * 8-deep DIIS on X (FPS - SPF) X, eigensolve of X^T F X, P = C_occ C_occ^T,
   E = tr((Core + F) P) + E_nuc, stop when ||P - P_old||_F < ``conver``.
 
-Every matrix stays on the device (float64): the Fock update runs in libmmdg.so,
-DIIS / eigensolve / products in cuBLAS / cuSOLVER through torch.  Extra keyword
-arguments (all default to the reference's behaviour):
+Every matrix stays on the device (float64): the Fock build and update run in
+libmmdg.so, the DIIS products in cuBLAS through torch; the (n+1)^2 DIIS system and
+the eigensolve of X^T F X run on the host cores (LAPACK dsyevd up to
+HOST_EIGH_MAX_N = 1024 functions, where it beats cuSOLVER; cuSOLVER above).  Extra
+keyword arguments (all default to the reference's behaviour):
 
 * ``fp32_below``  Schwarz-bound threshold under which shell quartets run in FP32
   (0: plain FP64 method);
@@ -20,7 +22,10 @@ arguments (all default to the reference's behaviour):
   Fock build F = Core + sym(G(P_guess));
 * ``guess_fallback``  with a guess: revert to the core guess when the DIIS error
   grows for 3 consecutive iterations;
-* ``maxiter``     iteration cap (reference: 100).
+* ``maxiter``     iteration cap (reference: 100);
+* ``process_group``  a torch.distributed group with one rank per GPU: each rank
+  digests its share of the shell quartets and one all-reduce of G completes every
+  Fock build (``mmd.distributed``); the rest of the SCF is replicated.
 """
 from __future__ import annotations
 
@@ -60,7 +65,7 @@ class SCF(object):
     """SCF methods for the molecule object (mmd/scf.py:8-180)."""
 
     def RHF(self, doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12, fp32_below=0.0, guess=None,
-            guess_fallback=True, maxiter=100, polish=False):
+            guess_fallback=True, maxiter=100, polish=False, process_group=None):
         """Restricted Hartree-Fock (mmd/scf.py:10-80): core-Hamiltonian start (or the
         density ``guess``, abandoned for the core guess after three growing DIIS
         errors when ``guess_fallback``), DIIS, stop on ||P - P_old||_F < conver.
@@ -69,7 +74,7 @@ class SCF(object):
         it in FP32; ``polish``: the returned energy from one non-incremental FP64 build
         of the final density.  Returns the energy (a numpy float64)."""
         state = self.scf_begin(DIIS=DIIS, direct=direct, acc2e=acc2e, fp32_below=fp32_below, guess=guess,
-                               guess_fallback=guess_fallback, maxiter=maxiter)
+                               guess_fallback=guess_fallback, maxiter=maxiter, process_group=process_group)
         t_start = time.perf_counter()
         for step in range(self.maxiter):
             state.iterate()
@@ -101,7 +106,7 @@ class SCF(object):
         return self.energy
 
     def scf_begin(self, DIIS=True, direct=False, acc2e=1e-12, fp32_below=0.0, guess=None, guess_fallback=True,
-                  maxiter=100, build=True):
+                  maxiter=100, build=True, process_group=None):
         """Integrals and the initial state of an RHF run; returns the iteration object."""
         self.is_converged = False
         self.delta_energy = 1e20
@@ -114,7 +119,30 @@ class SCF(object):
         self.fp32_below = float(fp32_below)
         if build or not getattr(self, "is_built", False):
             self.build(self.direct)
+        self._set_sharding(process_group if direct else None)
         return _RHFState(self, DIIS, guess, guess_fallback)
+
+    def _set_sharding(self, group):
+        """Sharded Fock builds over ``group`` (one GPU per rank), or none."""
+        old = getattr(self, "_sharded", None)
+        if old is not None:
+            old.close()
+            self._sharded = None
+        if group is not None:
+            import torch.distributed as dist
+            if dist.get_world_size(group) > 1:
+                from .distributed import ShardedFock
+                self._sharded = ShardedFock(self.context, group)
+                return
+        if self.context.nparts > 1:  # a shared context left sharded by another run
+            self.context.set_partition(0, 1)
+
+    def _fock_build(self, dP, tol, fp32_below):
+        """Unsymmetrised G(dP) of the whole molecule (sharded over ranks if set up)."""
+        sh = getattr(self, "_sharded", None)
+        if sh is not None:
+            return sh.fock(dP, tol=tol, fp32_below=fp32_below)
+        return self.context.fock(dP, tol=tol, fp32_below=fp32_below)
 
     def polished_energy(self):
         """E(P) = tr((H + F(P)) P) + E_nuc from one non-incremental FP64 Fock build of
@@ -126,7 +154,7 @@ class SCF(object):
         Core = self._dev["Core"]
         P = torch.as_tensor(np.ascontiguousarray(np.real(np.asarray(self.P)), dtype=np.float64), device=Core.device)
         if getattr(self, "direct", False):
-            G = ctx.fock(P.reshape(-1), tol=self.scrTol, fp32_below=0.0).view(self.nbasis, self.nbasis)
+            G = self._fock_build(P.reshape(-1), self.scrTol, 0.0).view(self.nbasis, self.nbasis)
             F = Core + 0.5 * (G + G.T)
         else:
             F = self._conventional_fock(P)
@@ -140,13 +168,13 @@ class SCF(object):
         t0 = time.perf_counter()
         dP = (P - P_old).contiguous().view(-1)
         prof = getattr(self, "_fock_profile", None)
-        if prof is not None:  # per-class device times and counts (measurement)
+        if prof is not None and getattr(self, "_sharded", None) is None:  # per-class times and counts
             G, ms, cnt = ctx.fock_timed(dP, tol=self.scrTol, fp32_below=self.fp32_below)
             prof["class_ms"] = prof.get("class_ms", 0.0) + ms.astype(np.float64)
             prof["counts"] = prof.get("counts", 0) + cnt.astype(np.float64)
             prof["builds"] = prof.get("builds", 0) + 1
         else:
-            G = ctx.fock(dP, tol=self.scrTol, fp32_below=self.fp32_below)
+            G = self._fock_build(dP, self.scrTol, self.fp32_below)
         self.fock_builds += 1
         self.fock_time += time.perf_counter() - t0
         G = G.view(self.nbasis, self.nbasis)

@@ -57,7 +57,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 GEN_DIR = os.path.join(REF_OUT, "gen")
 PKG_DIR = os.path.join(REF_OUT, "mmd", "integrals")
-DEFAULT_REFERENCE = os.environ.get("MMD_REFERENCE", "/root/reference")
+# the reference tree: --reference or $MMD_REFERENCE (required to cythonize)
+DEFAULT_REFERENCE = os.environ.get("MMD_REFERENCE")
 
 # modules on the hot path (plus onee, whose ``_boys`` hook test012 uses)
 HOT_MODULES = ("twoe", "fock", "onee")
@@ -153,6 +154,11 @@ def main(argv=None) -> int:
     args = ap.parse_args(argv)
 
     modules = ALL_MODULES if args.full else HOT_MODULES
+    if (not args.compile or args.full) and not args.reference:
+        if args.full or not os.path.isdir(GEN_DIR):
+            ap.error("the reference tree is required: pass --reference DIR or set MMD_REFERENCE")
+        print("no reference tree given (--reference / MMD_REFERENCE); compiling generated C only", file=sys.stderr)
+        args.compile = True
     if not args.compile:
         if not os.path.isdir(os.path.join(args.reference, "cython")):
             print(f"reference not found at {args.reference}; compiling generated C only", file=sys.stderr)

@@ -216,10 +216,36 @@ void oracle_screen(long N, const oracle_bfs* B, double* screen) {
     for (long q = 0; q < p + 1; ++q) screen[p * (p + 1) / 2 + q] = oracle_eri_flat(B, p, q, p, q);
 }
 
-/* formPT (cython/fock.pyx:13-87) for a real density difference dP = P - P_old.
+/* formPT (cython/fock.pyx:13-87) for a real density difference dP = P - P_old,
+ * restricted to the canonical bra pairs ij in [ij_lo, ij_hi) and, when `owner` is
+ * given, to the function quartets whose shell quartet belongs to `part`.  The
+ * restriction is test support (parallel checks and the sharded Fock build): the
+ * loop body is the reference's.  Ownership: function f lies in shell func_shell[f]
+ * (0..S-1, one molecule); a shell pair (s1 >= s2) has the canonical index
+ * s1(s1+1)/2 + s2; a shell quartet belongs to owner[] of its pair with the larger
+ * canonical index (owner[] is indexed by canonical pair index).
  * G (N*N, zeroed here) receives the unsymmetrised two-electron Fock update. */
-long oracle_formPT(long N, const oracle_bfs* B, const double* P, const double* P_old, const double* screen, double tol,
-                   double* G) {
+static long formPT_impl(long N, const oracle_bfs* B, const double* eri_table, const double* P, const double* P_old,
+                        const double* screen, double tol, double* G, long ij_lo, long ij_hi, const long* func_shell,
+                        const int* owner, int part);
+
+long oracle_formPT_part(long N, const oracle_bfs* B, const double* P, const double* P_old, const double* screen,
+                        double tol, double* G, long ij_lo, long ij_hi, const long* func_shell, const int* owner,
+                        int part) {
+  return formPT_impl(N, B, NULL, P, P_old, screen, tol, G, ij_lo, ij_hi, func_shell, owner, part);
+}
+
+/* formPT with the ERIs read from a table of the unique quartets in doERIs loop order
+ * (eri_table[ij(ij+1)/2 + kl], as oracle_eri_unique writes them) instead of being
+ * recomputed: the same values, so the same G; test support for large checks. */
+long oracle_formPT_table(long N, const double* eri_table, const double* P, const double* P_old, const double* screen,
+                         double tol, double* G) {
+  return formPT_impl(N, NULL, eri_table, P, P_old, screen, tol, G, 0, N * (N + 1) / 2, NULL, NULL, 0);
+}
+
+static long formPT_impl(long N, const oracle_bfs* B, const double* eri_table, const double* P, const double* P_old,
+                        const double* screen, double tol, double* G, long ij_lo, long ij_hi, const long* func_shell,
+                        const int* owner, int part) {
   double* dP = (double*)malloc(sizeof(double) * N * N);
   for (long x = 0; x < N * N; ++x) {
     dP[x] = P[x] - P_old[x];
@@ -228,13 +254,19 @@ long oracle_formPT(long N, const oracle_bfs* B, const double* P, const double* P
   long computed = 0;
 #define D(a, b) dP[(a) * N + (b)]
 #define GG(a, b) G[(a) * N + (b)]
+#define SPAIR(x, y) ((x) >= (y) ? (x) * ((x) + 1) / 2 + (y) : (y) * ((y) + 1) / 2 + (x))
   for (long i = 0; i < N; ++i)
     for (long j = 0; j < i + 1; ++j) {
       long ij = i * (i + 1) / 2 + j;
+      if (ij < ij_lo || ij >= ij_hi) continue;
       for (long k = 0; k < N; ++k)
         for (long l = 0; l < k + 1; ++l) {
           long kl = k * (k + 1) / 2 + l;
           if (ij < kl) continue;
+          if (owner) {
+            long c1 = SPAIR(func_shell[i], func_shell[j]), c2 = SPAIR(func_shell[k], func_shell[l]);
+            if (owner[c1 >= c2 ? c1 : c2] != part) continue;
+          }
           double bound = sqrt(screen[ij]) * sqrt(screen[kl]);
           double v[6] = {fabs(4 * D(i, j)), fabs(4 * D(k, l)), fabs(D(i, k)), fabs(D(i, l)), fabs(D(j, k)), fabs(D(j, l))};
           double dmax = v[0];
@@ -245,7 +277,8 @@ long oracle_formPT(long N, const oracle_bfs* B, const double* P, const double* P
           double s12 = (i == j) ? 1.0 : 2.0;
           double s34 = (k == l) ? 1.0 : 2.0;
           double s12_34 = (i == k) ? ((j == l) ? 1.0 : 2.0) : 2.0;
-          double eri = s12 * s34 * s12_34 * oracle_eri_flat(B, i, j, k, l);
+          double eri = s12 * s34 * s12_34 *
+                       (eri_table ? eri_table[ij * (ij + 1) / 2 + kl] : oracle_eri_flat(B, i, j, k, l));
           ++computed;
           GG(i, j) += D(k, l) * eri;
           GG(k, l) += D(i, j) * eri;
@@ -255,8 +288,180 @@ long oracle_formPT(long N, const oracle_bfs* B, const double* P, const double* P
           GG(k, j) += -0.25 * D(i, l) * eri;
         }
     }
+#undef SPAIR
 #undef D
 #undef GG
   free(dP);
   return computed;
+}
+
+/* formPT (cython/fock.pyx:13-87) over every function quartet. */
+long oracle_formPT(long N, const oracle_bfs* B, const double* P, const double* P_old, const double* screen, double tol,
+                   double* G) {
+  return oracle_formPT_part(N, B, P, P_old, screen, tol, G, 0, N * (N + 1) / 2, NULL, NULL, 0);
+}
+
+/* The unique ERIs of doERIs (cython/twoe.pyx:12-31) with canonical bra pair ij in
+ * [ij_lo, ij_hi), in loop order (ij ascending, then kl = 0..ij): out receives
+ * sum_{ij} (ij+1) values.  Test support: splits doERIs over processes. */
+void oracle_eri_unique(long N, const oracle_bfs* B, long ij_lo, long ij_hi, double* out) {
+  long o = 0;
+  for (long i = 0; i < N; ++i)
+    for (long j = 0; j < i + 1; ++j) {
+      long ij = i * (i + 1) / 2 + j;
+      if (ij < ij_lo || ij >= ij_hi) continue;
+      for (long k = 0; k < N; ++k)
+        for (long l = 0; l < k + 1; ++l) {
+          long kl = k * (k + 1) / 2 + l;
+          if (kl > ij) continue;
+          out[o++] = oracle_eri_flat(B, i, j, k, l);
+        }
+    }
+}
+
+/* ------------------------------------------------ memoised shell-quartet ERIs
+ * All component ERIs of four shells at once, with the Hermite E (util.pxi:13-28)
+ * and R (util.pxi:33-50) recursions memoised per primitive pair / primitive
+ * quartet.  Each memo entry is computed by the same expression from the same
+ * child values as the plain recursion, and every sum runs in the order of
+ * oracle_eri / oracle_primitive_eri, so the results equal oracle_eri_flat bit for
+ * bit (pinned in the CPU tests); only repeated evaluations are skipped.  Shells
+ * are lists of functions that share origin and exponents (one Cartesian shell). */
+#define ORACLE_EMAX 3 /* i, j <= 2 */
+#define ORACLE_TMAX 6
+typedef struct {
+  double Qx, a, b;
+  double val[ORACLE_EMAX][ORACLE_EMAX][ORACLE_TMAX];
+  char have[ORACLE_EMAX][ORACLE_EMAX][ORACLE_TMAX];
+} emo;
+
+static double emo_E(emo* m, int i, int j, int t) {
+  double p = m->a + m->b;
+  double u = m->a * m->b / p;
+  if (t < 0 || t > i + j) return 0.0;
+  if (m->have[i][j][t]) return m->val[i][j][t];
+  double r;
+  if (i == 0 && j == 0 && t == 0)
+    r = exp(-u * m->Qx * m->Qx);
+  else if (j == 0)
+    r = (1.0 / (2.0 * p)) * emo_E(m, i - 1, j, t - 1) - (u * m->Qx / m->a) * emo_E(m, i - 1, j, t) +
+        (t + 1) * emo_E(m, i - 1, j, t + 1);
+  else
+    r = (1.0 / (2.0 * p)) * emo_E(m, i, j - 1, t - 1) + (u * m->Qx / m->b) * emo_E(m, i, j - 1, t) +
+        (t + 1) * emo_E(m, i, j - 1, t + 1);
+  m->val[i][j][t] = r;
+  m->have[i][j][t] = 1;
+  return r;
+}
+
+#define ORACLE_RMAX 9 /* t, u, v, n <= 8 */
+typedef struct {
+  double p, PCx, PCy, PCz, RPC;
+  double val[ORACLE_RMAX][ORACLE_RMAX][ORACLE_RMAX][ORACLE_RMAX];
+  char have[ORACLE_RMAX][ORACLE_RMAX][ORACLE_RMAX][ORACLE_RMAX];
+} rmo;
+
+static double rmo_R(rmo* m, int t, int u, int v, int n) {
+  if (m->have[t][u][v][n]) return m->val[t][u][v][n];
+  double T = m->p * m->RPC * m->RPC;
+  double val = 0.0;
+  if (t == 0 && u == 0 && v == 0) {
+    val += pow(-2.0 * m->p, n) * oracle_boys((double)n, T);
+  } else if (t == 0 && u == 0) {
+    if (v > 1) val += (v - 1) * rmo_R(m, t, u, v - 2, n + 1);
+    val += m->PCz * rmo_R(m, t, u, v - 1, n + 1);
+  } else if (t == 0) {
+    if (u > 1) val += (u - 1) * rmo_R(m, t, u - 2, v, n + 1);
+    val += m->PCy * rmo_R(m, t, u - 1, v, n + 1);
+  } else {
+    if (t > 1) val += (t - 1) * rmo_R(m, t - 2, u, v, n + 1);
+    val += m->PCx * rmo_R(m, t - 1, u, v, n + 1);
+  }
+  m->val[t][u][v][n] = val;
+  m->have[t][u][v][n] = 1;
+  return val;
+}
+
+/* out[((x*nb + y)*nc + z)*nd + w] = ERI(fa[x], fb[y], fc[z], fd[w]) */
+void oracle_eri_shell(const oracle_bfs* B, const long* fa, long na, const long* fb, long nb, const long* fc, long nc,
+                      const long* fd, long nd, double* out) {
+  oracle_basis A, Bb, C, Dd;
+  bfs_get(B, fa[0], &A);
+  bfs_get(B, fb[0], &Bb);
+  bfs_get(B, fc[0], &C);
+  bfs_get(B, fd[0], &Dd);
+  const long ntot = na * nb * nc * nd;
+  for (long x = 0; x < ntot; ++x) out[x] = 0.0;
+  emo* e1 = (emo*)malloc(sizeof(emo) * 3);
+  emo* e2 = (emo*)malloc(sizeof(emo) * 3);
+  rmo* r = (rmo*)malloc(sizeof(rmo));
+  for (long ja = 0; ja < A.num_exps; ++ja)
+    for (long jb = 0; jb < Bb.num_exps; ++jb) {
+      const double a = A.exps[ja], b = Bb.exps[jb];
+      for (int dim = 0; dim < 3; ++dim) {
+        memset(e1[dim].have, 0, sizeof(e1[dim].have));
+        e1[dim].Qx = A.origin[dim] - Bb.origin[dim];
+        e1[dim].a = a;
+        e1[dim].b = b;
+      }
+      for (long jc = 0; jc < C.num_exps; ++jc)
+        for (long jd = 0; jd < Dd.num_exps; ++jd) {
+          const double c = C.exps[jc], d = Dd.exps[jd];
+          for (int dim = 0; dim < 3; ++dim) {
+            memset(e2[dim].have, 0, sizeof(e2[dim].have));
+            e2[dim].Qx = C.origin[dim] - Dd.origin[dim];
+            e2[dim].a = c;
+            e2[dim].b = d;
+          }
+          /* geometry of oracle_primitive_eri, the same expressions */
+          double p = a + b, q = c + d;
+          double alpha = p * q / (p + q);
+          double Px = (a * A.origin[0] + b * Bb.origin[0]) / p, Py = (a * A.origin[1] + b * Bb.origin[1]) / p,
+                 Pz = (a * A.origin[2] + b * Bb.origin[2]) / p;
+          double Qx = (c * C.origin[0] + d * Dd.origin[0]) / q, Qy = (c * C.origin[1] + d * Dd.origin[1]) / q,
+                 Qz = (c * C.origin[2] + d * Dd.origin[2]) / q;
+          double RPQ = sqrt(pow(Px - Qx, 2) + pow(Py - Qy, 2) + pow(Pz - Qz, 2));
+          memset(r->have, 0, sizeof(r->have));
+          r->p = alpha;
+          r->PCx = Px - Qx;
+          r->PCy = Py - Qy;
+          r->PCz = Pz - Qz;
+          r->RPC = RPQ;
+          const double pref = 2.0 * pow(ORACLE_PI, 2.5) / (p * q * sqrt(p + q));
+          for (long x = 0; x < na; ++x)
+            for (long y = 0; y < nb; ++y)
+              for (long z = 0; z < nc; ++z)
+                for (long w = 0; w < nd; ++w) {
+                  oracle_basis fa_, fb_, fc_, fd_;
+                  bfs_get(B, fa[x], &fa_);
+                  bfs_get(B, fb[y], &fb_);
+                  bfs_get(B, fc[z], &fc_);
+                  bfs_get(B, fd[w], &fd_);
+                  const long l1 = fa_.shell[0], m1 = fa_.shell[1], n1 = fa_.shell[2];
+                  const long l2 = fb_.shell[0], m2 = fb_.shell[1], n2 = fb_.shell[2];
+                  const long l3 = fc_.shell[0], m3 = fc_.shell[1], n3 = fc_.shell[2];
+                  const long l4 = fd_.shell[0], m4 = fd_.shell[1], n4 = fd_.shell[2];
+                  double val = 0.0;
+                  for (long t = 0; t < l1 + l2 + 1; ++t)
+                    for (long u = 0; u < m1 + m2 + 1; ++u)
+                      for (long v = 0; v < n1 + n2 + 1; ++v)
+                        for (long tau = 0; tau < l3 + l4 + 1; ++tau)
+                          for (long nu = 0; nu < m3 + m4 + 1; ++nu)
+                            for (long phi = 0; phi < n3 + n4 + 1; ++phi)
+                              val += emo_E(&e1[0], (int)l1, (int)l2, (int)t) * emo_E(&e1[1], (int)m1, (int)m2, (int)u) *
+                                     emo_E(&e1[2], (int)n1, (int)n2, (int)v) *
+                                     emo_E(&e2[0], (int)l3, (int)l4, (int)tau) *
+                                     emo_E(&e2[1], (int)m3, (int)m4, (int)nu) *
+                                     emo_E(&e2[2], (int)n3, (int)n4, (int)phi) * pow(-1.0, (double)(tau + nu + phi)) *
+                                     rmo_R(r, (int)(t + tau), (int)(u + nu), (int)(v + phi), 0);
+                  val *= pref;
+                  out[((x * nb + y) * nc + z) * nd + w] +=
+                      fa_.norm[ja] * fb_.norm[jb] * fc_.norm[jc] * fd_.norm[jd] * fa_.coefs[ja] * fb_.coefs[jb] *
+                      fc_.coefs[jc] * fd_.coefs[jd] * val;
+                }
+        }
+    }
+  free(e1);
+  free(e2);
+  free(r);
 }

@@ -57,6 +57,14 @@ def lib():
         L.oracle_screen.argtypes = [l, p, p]
         L.oracle_formPT.restype = l
         L.oracle_formPT.argtypes = [l, p, p, p, p, d, p]
+        L.oracle_formPT_part.restype = l
+        L.oracle_formPT_part.argtypes = [l, p, p, p, p, d, p, l, l, p, p, ctypes.c_int]
+        L.oracle_formPT_table.restype = l
+        L.oracle_formPT_table.argtypes = [l, p, p, p, p, d, p]
+        L.oracle_eri_unique.restype = None
+        L.oracle_eri_unique.argtypes = [l, p, l, l, p]
+        L.oracle_eri_shell.restype = None
+        L.oracle_eri_shell.argtypes = [p, p, l, p, l, p, l, p, l, p]
         _LIB = L
     return _LIB
 
@@ -168,3 +176,166 @@ def reference_modules():
     except ImportError:
         return None
     return twoe, fock
+
+
+# ------------------------------------------------------------------ partial / parallel forms
+def formPT_part(P, P_old, bfs, nbasis, screen, tol, ij_lo=0, ij_hi=None, func_shell=None, owner=None, part=0):
+    """formPT restricted to canonical bra pairs ij in [ij_lo, ij_hi) and, with
+    ``owner`` (per canonical shell-pair index s1(s1+1)/2+s2) and ``func_shell`` (shell
+    of every function), to the shell quartets owned by ``part`` (the owner of the
+    quartet's pair with the larger canonical index).  Returns the real partial G."""
+    N = int(nbasis)
+    npair = N * (N + 1) // 2
+    ij_hi = npair if ij_hi is None else int(ij_hi)
+    Pr = np.ascontiguousarray(np.real(np.asarray(P)), dtype=np.float64)
+    Po = np.ascontiguousarray(np.real(np.asarray(P_old)), dtype=np.float64)
+    if isinstance(screen, dict):
+        scr = np.array([screen[i] for i in range(npair)], dtype=np.float64)
+    else:
+        scr = np.ascontiguousarray(screen, dtype=np.float64)
+    G = np.zeros((N, N))
+    pk = _Pack(bfs)
+    fs = ow = None
+    if owner is not None:
+        fs = np.ascontiguousarray(func_shell, dtype=np.int64)
+        ow = np.ascontiguousarray(owner, dtype=np.int32)
+    lib().oracle_formPT_part(N, pk.ptr, Pr.ctypes.data, Po.ctypes.data, scr.ctypes.data, float(tol), G.ctypes.data,
+                             int(ij_lo), ij_hi, None if fs is None else fs.ctypes.data,
+                             None if ow is None else ow.ctypes.data, int(part))
+    return G
+
+
+def formPT_table(P, P_old, eri_table, nbasis, screen, tol):
+    """formPT (cython/fock.pyx:13-87) reading the ERIs from ``eri_table``, the unique
+    quartets in doERIs loop order (``eri_unique`` / ``parallel_eri_unique``); real G."""
+    N = int(nbasis)
+    npair = N * (N + 1) // 2
+    tab = np.ascontiguousarray(eri_table, dtype=np.float64)
+    assert tab.size == npair * (npair + 1) // 2
+    Pr = np.ascontiguousarray(np.real(np.asarray(P)), dtype=np.float64)
+    Po = np.ascontiguousarray(np.real(np.asarray(P_old)), dtype=np.float64)
+    scr = np.ascontiguousarray([screen[i] for i in range(npair)] if isinstance(screen, dict) else screen,
+                               dtype=np.float64)
+    G = np.zeros((N, N))
+    lib().oracle_formPT_table(N, tab.ctypes.data, Pr.ctypes.data, Po.ctypes.data, scr.ctypes.data, float(tol),
+                              G.ctypes.data)
+    return G
+
+
+def eri_unique(bfs, ij_lo, ij_hi):
+    """The unique ERIs (ij|kl), kl <= ij, for canonical ij in [ij_lo, ij_hi), in doERIs
+    loop order (twoe.pyx:12-31)."""
+    N = len(bfs)
+    n = sum(ij + 1 for ij in range(int(ij_lo), int(ij_hi)))
+    out = np.zeros(max(n, 1))
+    pk = _Pack(bfs)
+    lib().oracle_eri_unique(N, pk.ptr, int(ij_lo), int(ij_hi), out.ctypes.data)
+    return out[:n]
+
+
+def eri_shell(bfs, fa, fb, fc, fd):
+    """All component ERIs of four shells given as function-index lists (each list one
+    Cartesian shell: same origin and exponents); array [len(fa), len(fb), len(fc), len(fd)],
+    equal bit for bit to ERI() per function quartet."""
+    arrs = [np.ascontiguousarray(x, dtype=np.int64) for x in (fa, fb, fc, fd)]
+    out = np.zeros(tuple(len(a) for a in arrs))
+    pk = _Pack(bfs)
+    lib().oracle_eri_shell(pk.ptr, arrs[0].ctypes.data, len(arrs[0]), arrs[1].ctypes.data, len(arrs[1]),
+                           arrs[2].ctypes.data, len(arrs[2]), arrs[3].ctypes.data, len(arrs[3]), out.ctypes.data)
+    return out
+
+
+class _Plain:
+    """A Basis-like record carrying already-normalised data (no renormalisation)."""
+
+    def __init__(self, origin, shell, num_exps, exps, coefs, norm):
+        self.origin, self.shell, self.num_exps = origin, shell, num_exps
+        self.exps, self.coefs, self.norm = exps, coefs, norm
+
+
+def _plain(bfs):
+    return [(list(map(float, b.origin)), [int(x) for x in b.shell], int(b.num_exps),
+             list(map(float, np.asarray(b.exps)[: int(b.num_exps)])),
+             list(map(float, np.asarray(b.coefs)[: int(b.num_exps)])),
+             list(map(float, np.asarray(b.norm)[: int(b.num_exps)]))) for b in bfs]
+
+
+_WB = None
+
+
+def _w_init(data):
+    global _WB
+    _WB = [_Plain(*t) for t in data]
+
+
+def _w_formPT(args):
+    P, Po, N, scr, tol, lo, hi = args
+    return formPT_part(P, Po, _WB, N, scr, tol, lo, hi)
+
+
+def _w_unique(args):
+    lo, hi = args
+    return eri_unique(_WB, lo, hi)
+
+
+def _w_shell(args):
+    return [eri_shell(_WB, *q) for q in args]
+
+
+def _ij_ranges(N, parts):
+    """Contiguous canonical-ij ranges holding about equal numbers of quartets (ij+1 each)."""
+    npair = N * (N + 1) // 2
+    cum = np.cumsum(np.arange(1, npair + 1, dtype=np.float64))
+    cuts = [0] + [int(np.searchsorted(cum, cum[-1] * k / parts)) for k in range(1, parts)] + [npair]
+    return [(a, b) for a, b in zip(cuts[:-1], cuts[1:]) if b > a]
+
+
+def _pool(bfs, nproc):
+    import multiprocessing as mp
+    nproc = int(nproc or os.cpu_count() or 1)
+    # spawn: safe after CUDA has been initialised in the parent
+    return mp.get_context("spawn").Pool(nproc, initializer=_w_init, initargs=(_plain(bfs),)), nproc
+
+
+def parallel_formPT(P, P_old, bfs, nbasis, screen, tol, nproc=None):
+    """formPT over every function quartet, split into ij ranges over processes; real G."""
+    N = int(nbasis)
+    scr = np.array([screen[i] for i in range(N * (N + 1) // 2)]) if isinstance(screen, dict) else np.asarray(screen)
+    pool, n = _pool(bfs, nproc)
+    with pool:
+        parts = pool.map(_w_formPT, [(np.real(P), np.real(P_old), N, scr, tol, lo, hi)
+                                     for lo, hi in _ij_ranges(N, 4 * n)])
+    return np.sum(parts, axis=0)
+
+
+def parallel_eri_unique(bfs, nproc=None):
+    """All unique ERIs of doERIs in loop order, computed over processes."""
+    N = len(bfs)
+    pool, n = _pool(bfs, nproc)
+    with pool:
+        parts = pool.map(_w_unique, _ij_ranges(N, 4 * n))
+    return np.concatenate(parts)
+
+
+def parallel_eri_shells(bfs, quartets, nproc=None):
+    """eri_shell for a list of (fa, fb, fc, fd) function-index lists, over processes."""
+    pool, n = _pool(bfs, nproc)
+    chunks = [quartets[k::4 * n] for k in range(4 * n)]
+    with pool:
+        res = pool.map(_w_shell, chunks)
+    out = [None] * len(quartets)
+    for k, r in enumerate(res):
+        for m, v in enumerate(r):
+            out[k + m * 4 * n] = v
+    return out
+
+
+def unique_index(N):
+    """(i, j, k, l) arrays of the unique quartets in doERIs loop order (ij ascending,
+    then kl = 0..ij), matching eri_unique / parallel_eri_unique."""
+    ii, jj = np.tril_indices(N)
+    order = np.argsort(ii * (ii + 1) // 2 + jj, kind="stable")
+    ii, jj = ii[order], jj[order]
+    npair = len(ii)
+    a, b = np.tril_indices(npair)  # a = ij (row), b = kl <= ij, row-major: ij ascending then kl
+    return ii[a], jj[a], ii[b], jj[b]

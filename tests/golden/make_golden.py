@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Runs only where the reference tree is present (it reads /root/reference, or
-$MMD_REFERENCE).  It lays out a shimmed, compiled copy of the reference package
+Runs only where the reference tree is present (its path in $MMD_REFERENCE, which
+is required).  It lays out a shimmed, compiled copy of the reference package
 with ``oracle/build_ref.py --full`` (the same three shims), imports it, and dumps
 the reference's own outputs:
 
@@ -38,7 +38,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE = os.environ.get("MMD_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("MMD_REFERENCE", "")
 REFCOPY = os.environ.get("MMD_REFCOPY", "/tmp/mmd_golden_ref")
 
 
@@ -51,6 +51,8 @@ def _load_clusters():
 
 
 def _prepare_reference():
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "cython")):
+        raise SystemExit("set MMD_REFERENCE to the reference tree (the directory holding cython/ and mmd/)")
     if not os.path.isdir(os.path.join(REFCOPY, "mmd", "integrals")):
         subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "build_ref.py"),
                                "--reference", REFERENCE, "--full", REFCOPY])

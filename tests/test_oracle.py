@@ -142,3 +142,73 @@ def test_mp2_oracle_matches_reference():
         assert abs(X.mp2_spatial(C, e, d["TwoE"], nocc) + c["energy"] - c["emp2_spatial"]) < 1e-10
         dbl = X.spin_integrals(C, d["TwoE"])
         assert abs(X.mp2_spin(e, dbl, 2 * nocc) + c["energy"] - c["emp2_spin"]) < 1e-10
+
+
+# ------------------------------------------------------------------ partial / fast oracle forms
+def _shell_lists(bfs_mol):
+    """Function-index lists of the shells of a Molecule's basis (the product's grouping)."""
+    from mmd.integrals.shells import shells_from_bfs
+    ss = shells_from_bfs(bfs_mol)
+    return [[int(f) for f in row if f >= 0] for row in ss.func], ss
+
+
+def test_memoised_shell_eri_equals_per_function_eri_bitwise(golden):
+    """oracle eri_shell (memoised E and R, whole shells) gives exactly ERI() of every
+    component quartet: the same recursions and summation order, evaluated once."""
+    from mmd.molecule import Molecule
+    d = golden("mol_water_631gss.npz")
+    bfs = _raw_bfs(d)
+    shells, _ = _shell_lists(Molecule(str(d["geometry"]), "6-31gss").bfs)
+    rng = np.random.default_rng(3)
+    picks = [tuple(int(x) for x in rng.integers(0, len(shells), 4)) for _ in range(24)]
+    picks += [(5, 5, 5, 5), (5, 4, 5, 2)]  # the d shell of O: (dd|dd) and (dp|ds)
+    for q in picks:
+        fl = [shells[s] for s in q]
+        v = O.eri_shell(bfs, *fl)
+        for x, i in enumerate(fl[0]):
+            for y, j in enumerate(fl[1]):
+                for z, k in enumerate(fl[2]):
+                    for w, l in enumerate(fl[3]):
+                        assert v[x, y, z, w] == O.ERI(bfs[i], bfs[j], bfs[k], bfs[l]), (q, x, y, z, w)
+
+
+def test_ranged_unique_eris_equal_doERIs(golden):
+    d = golden("mol_water_sto3g.npz")
+    bfs = _raw_bfs(d)
+    N = len(bfs)
+    T = O.doERIs(N, np.zeros((N, N, N, N)), bfs)
+    i, j, k, l = O.unique_index(N)
+    npair = N * (N + 1) // 2
+    parts = [O.eri_unique(bfs, a, b) for a, b in ((0, 9), (9, 20), (20, npair))]
+    assert np.array_equal(np.concatenate(parts), T[i, j, k, l])
+    assert np.max(np.abs(T[i, j, k, l] - d["TwoE"][i, j, k, l])) < 1e-13
+    # formPT from the table of those ERIs equals formPT recomputing them, bit for bit
+    k0 = 0
+    while f"formPT{k0}_G" in d:
+        P, Po = d[f"formPT{k0}_P"], d[f"formPT{k0}_Pold"]
+        Gt = O.formPT_table(P, Po, T[i, j, k, l], N, d["screen"], 1e-12)
+        assert np.array_equal(Gt, O.formPT(P, Po, bfs, N, d["screen"], 1e-12).real)
+        k0 += 1
+
+
+def test_partial_formPT_adds_up_to_formPT(golden):
+    """formPT restricted to ij ranges, or to the shell quartets of each part of a
+    shell-pair partition, adds up to the full formPT (the reference's records)."""
+    from mmd.distributed import function_shells, partition_shell_pairs
+    from mmd.molecule import Molecule
+    d = golden("mol_water_631g.npz")
+    bfs = _raw_bfs(d)
+    N = int(d["nbasis"])
+    P, Po = d["formPT0_P"], d["formPT0_Pold"]
+    ref = d["formPT0_G"]
+    npair = N * (N + 1) // 2
+    G = sum(O.formPT_part(P, Po, bfs, N, d["screen"], 1e-12, a, b) for a, b in ((0, 30), (30, 61), (61, npair)))
+    assert np.max(np.abs(G - ref)) < 1e-13
+    _, ss = _shell_lists(Molecule(str(d["geometry"]), "6-31g").bfs)
+    fs = function_shells(ss)
+    for world in (2, 3):
+        owner = partition_shell_pairs(ss, world)
+        parts = [O.formPT_part(P, Po, bfs, N, d["screen"], 1e-12, func_shell=fs, owner=owner, part=r)
+                 for r in range(world)]
+        assert all(np.abs(p).max() > 0 for p in parts)
+        assert np.max(np.abs(sum(parts) - ref)) < 1e-13
