@@ -19,8 +19,11 @@ Printed (rank 0, one JSON line):
   e2e        the same metric through the reference-facing API formPT(P, P_old,
              bfs, nbasis, screen, tol) with host arrays in and out
   time_to_converge_s  Molecule(geometry, basis).RHF(direct=True) wall time (conver 1e-8)
-  roofline   FP64-pipe roofline of the dominant class kernel (live CUDA events,
-             model FLOPs of mmd/flop_model.py, peak measured live by mmdg_measure_peaks)
+  roofline   FP64-pipe roofline of the dominant class kernel (live CUDA events; the
+             FP64 FLOPs the kernels issue, counted from the code's structure and the
+             build's counters by mmd/flop_model.py, with the algorithm's useful FLOPs
+             and the dense reference model beside them, per class; peak measured
+             live by mmdg_measure_peaks)
   cpu_baseline  the reference's Cython formPT (oracle/_ref) on the host cores, a
              bounded sample extrapolated to this workload (see cpu_sample())
 
@@ -504,6 +507,52 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=COMBINED_FP32_B
             "plain_fp64_energy_error_vs_oracle": float(plain_mol.energy) - E_oracle}
 
 
+def fp64_roofline(class_ms, counts, builds, fp64_peak):
+    """FP64-pipe roofline of the Fock build from per-class CUDA-event times and counters.
+
+    Per class: ``issued`` = FP64 FLOPs the kernel issues (flop_model.issued_flops:
+    chunk passes, padded lanes and all), ``useful`` = the algorithm's own FLOPs (no
+    recomputation or padding), ``model`` = the dense reference count; each as TFLOP/s
+    and as a fraction of the measured DFMA peak.  The headline is the dominant
+    class's issued rate."""
+    import numpy as np
+    from mmd import flop_model as F
+    per = {}
+    tot = {"issued": 0.0, "useful": 0.0, "model": 0.0}
+    for c, ms, row in zip(F.CLASSES, class_ms, counts):
+        if ms <= 0:
+            continue
+        fl = {"issued": F.issued_flops(c, row), "useful": F.useful_flops(c, row),
+              "model": F.class_flops(c, row[2], row[0])}
+        for k in tot:
+            tot[k] += fl[k]
+        t = ms / 1e3
+        per["%d%d%d%d" % c] = {"ms_per_build": float(ms) / builds, "kernel": F.fock_kernel(c),
+                               **{f"{k}_frac": fl[k] / t / 1e12 / fp64_peak for k in fl}}
+    dom = int(np.argmax(class_ms))
+    c = F.CLASSES[dom]
+    key = "%d%d%d%d" % c
+    row = counts[dom]
+    issued = F.issued_flops(c, row)
+    t = class_ms[dom] / 1e3
+    achieved = issued / t / 1e12
+    kern = "k_fock_warp<MDW_%s,double>" % key if F.fock_kernel(c) == "warp" else "k_fock<MD_%s,double>" % key
+    T = float(np.sum(class_ms)) / 1e3
+    return {"bound": "fp64", "kernel": kern, "class": key, "achieved": achieved, "peak": fp64_peak,
+            "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+            "flops": "issued FP64 FLOPs (2 per DFMA, 1 per DMUL/DADD) counted from the code and the build's "
+                     "counters; excludes the FP64 instructions inside CUDA's rsqrt/exp",
+            "flops_per_launch": issued / builds, "launch_ms": float(class_ms[dom]) / builds,
+            "useful_frac": F.useful_flops(c, row) / t / 1e12 / fp64_peak,
+            "model_frac": F.class_flops(c, row[2], row[0]) / t / 1e12 / fp64_peak,
+            "peak_source": "live DFMA probe mmdg_measure_peaks (MEASURED_PEAKS.json has no FP64 figure)",
+            "all_classes": {"fock_build_ms": float(np.sum(class_ms)) / builds,
+                            "issued_frac": tot["issued"] / T / 1e12 / fp64_peak,
+                            "useful_frac": tot["useful"] / T / 1e12 / fp64_peak,
+                            "model_frac": tot["model"] / T / 1e12 / fp64_peak},
+            "per_class": per}
+
+
 # ------------------------------------------------------------------------------ GPU arm
 def gpu_arm(args):
     import numpy as np
@@ -561,7 +610,7 @@ def gpu_arm(args):
     # class kernel timed alone by CUDA events (one stream), with its quartet counts
     ctx = mol.context
     class_ms = np.zeros(len(flop_model.CLASSES))
-    counts = np.zeros((len(flop_model.CLASSES), 3))
+    counts = np.zeros((len(flop_model.CLASSES), _native.NCOUNT))
     L2flush = flush
     for P_, Po_ in dens:
         L2flush.zero_()
@@ -569,27 +618,19 @@ def gpu_arm(args):
         class_ms += ms.astype(np.float64)
         counts += cnt.astype(np.float64)
     fq_per_build = float(counts[:, 0].sum()) / builds
-    # ---------------- roofline of the dominant class kernel
+    # ---------------- FP64 roofline: FLOPs the kernels issue (counted from the code's
+    # structure and the build's counters; ncu's DFMA/DMUL/DADD counters are the
+    # cross-check), the algorithm's useful FLOPs and the dense reference model
     fp64_peak, fp32_peak = _native.measure_peaks(ctx)
-    cls_flops = np.array([flop_model.class_flops(c, row[2], row[0]) for c, row in zip(flop_model.CLASSES, counts)])
-    cls_exec = np.array([flop_model.executed_flops_per_prim_quartet(*c) * row[2] + 12.0 * row[0]
-                         for c, row in zip(flop_model.CLASSES, counts)])
-    dom = int(np.argmax(class_ms))
-    dom_cls = flop_model.CLASSES[dom]
-    achieved = cls_flops[dom] / (class_ms[dom] / 1e3) / 1e12
+    roofline = fp64_roofline(class_ms, counts, builds, fp64_peak)
+    roofline["fp32_peak"] = fp32_peak
+    if WORKLOAD["n_water"] == 16:
+        key = roofline["class"]
+        roofline["traffic"] = DRAM_BYTES_PER_LAUNCH.get(key)
+        roofline["fp64_pipe_busy_ncu"] = FP64_PIPE_BUSY.get(key)
+    else:
+        roofline["traffic"] = None
     build_ms = float(class_ms.sum()) / builds  # class kernels timed one after another
-    all_achieved = float(cls_flops.sum()) / (float(class_ms.sum()) / 1e3) / 1e12
-    traffic = DRAM_BYTES_PER_LAUNCH.get("%d%d%d%d" % dom_cls) if WORKLOAD["n_water"] == 16 else None
-    roofline = {"bound": "fp64", "kernel": "k_fock<MD_%d%d%d%d,double>" % dom_cls, "achieved": achieved,
-                "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": traffic,
-                "traffic_note": "DRAM bytes of one iteration-1 launch (ncu); the kernel is FP64-pipe bound",
-                "fp64_pipe_busy_ncu": FP64_PIPE_BUSY.get("%d%d%d%d" % dom_cls) if WORKLOAD["n_water"] == 16 else None,
-                "peak_source": "live DFMA probe mmdg_measure_peaks (MEASURED_PEAKS.json has no FP64 figure)",
-                "flops_per_launch": float(cls_flops[dom]) / builds, "launch_ms": float(class_ms[dom]) / builds,
-                "all_classes": {"achieved": all_achieved, "frac": all_achieved / fp64_peak,
-                                "fock_build_ms": build_ms,
-                                "executed_achieved": float(cls_exec.sum()) / (float(class_ms.sum()) / 1e3) / 1e12},
-                "fp32_peak": fp32_peak}
     # ---------------- e2e through formPT with host arrays
     Ph = [(a.cpu().numpy(), b.cpu().numpy()) for a, b in dens]
     screen = mol.screen

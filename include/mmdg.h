@@ -30,6 +30,7 @@
  *                        every component of listed shell quartets.
  *   mmdg_set_partition <- the bra-pair loop of formPT (cython/fock.pyx:38-44) split
  *                        over GPUs: each rank digests the shell quartets it owns.
+ *   mmdg_ao2mo        <- the AO -> MO transform of PostSCF.ao2mo (mmd/postscf.py:26-27).
  */
 #ifndef MMDG_H
 #define MMDG_H
@@ -48,6 +49,7 @@ extern "C" {
 #define MMDG_LMAX 2          /* highest shell angular momentum (Cartesian d) */
 #define MMDG_MAX_COMP 6      /* Cartesian components of a d shell */
 #define MMDG_NCLASS 21       /* angular classes (la lb|lc ld), la>=lb, lc>=ld, (la,lb)>=(lc,ld) */
+#define MMDG_NCOUNT 5        /* per-class counters of a Fock build (mmdg_fock counts) */
 
 typedef struct mmdg_context mmdg_context;
 
@@ -131,9 +133,11 @@ int mmdg_device_bytes(mmdg_context* ctx, long long* bytes);
  *   tol       screening threshold (acc2e of RHF; reference default 1e-12)
  *   fp32_below  shell quartets whose Schwarz bound Q_ab*Q_cd is below this value are
  *             evaluated in FP32 (0 = all FP64, the plain method)
- *   counts    optional host array of 3*MMDG_NCLASS unsigned long long: per class the
- *             shell quartets, primitive quartets and function quartets computed
- *             (filled after a stream synchronisation; pass NULL to stay asynchronous)
+ *   counts    optional host array of MMDG_NCOUNT*MMDG_NCLASS unsigned long long: per
+ *             class the digested function quartets, shell quartets, primitive quartets,
+ *             bra-primitive passes and primitive quartets whose Boys function took the
+ *             asymptotic branch (filled after a stream synchronisation; pass NULL to
+ *             stay asynchronous)
  */
 int mmdg_fock(mmdg_context* ctx, const double* dP, double* G, double tol, double fp32_below,
               unsigned long long* counts, void* stream);
@@ -214,6 +218,13 @@ int mmdg_mlp_mse(const float* Y, const float* T, const float* mask, float* dY, d
 int mmdg_mlp_adam(float* w, void* w_bf16, const float* g, float* m, float* v, long long n, float lr, float b1,
                   float b2, float eps, int step, void* stream);
 int mmdg_mlp_to_bf16(const float* w, void* w_bf16, long long n, void* stream);
+
+/* AO -> MO transform of an ERI tensor (mmd/postscf.py:26-27, four einsums with the MO
+ * coefficients): eri_out[P,Q,R,S] = sum_pqrs C[p,P] C[q,Q] C[r,R] C[s,S] eri_in[p,q,r,s].
+ * All device arrays, C order: C is N x N (AO row, MO column), eri_in / eri_out / work
+ * are N^4 and distinct; eri_in is left unchanged, work is scratch.  Four FP64 quarter
+ * transforms (each contracts the last index and writes the new one first). */
+int mmdg_ao2mo(long long N, const double* C, const double* eri_in, double* eri_out, double* work, void* stream);
 
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);

@@ -45,7 +45,7 @@ def _sources():
     os.makedirs(BUILD, exist_ok=True)
     gen_md.generate(os.path.join(BUILD, "md_gen.cuh"))
     inst = gen_md.generate_instances(BUILD)
-    return [os.path.join(CSRC, "capi.cu"), os.path.join(CSRC, "noalloc.cu"), os.path.join(CSRC, "mlp.cu"), os.path.join(CSRC, "grad.cu")] + inst
+    return [os.path.join(CSRC, "capi.cu"), os.path.join(CSRC, "noalloc.cu"), os.path.join(CSRC, "mlp.cu"), os.path.join(CSRC, "grad.cu"), os.path.join(CSRC, "ao2mo.cu")] + inst
 
 
 def _deps():

@@ -583,7 +583,7 @@ extern "C" int mmdg_set_basis(mmdg_context* h, int nmol, const int* mol_nfunc, i
             h->d_E32.alloc(ne) == cudaSuccess && h->d_Q.alloc(h->npair) == cudaSuccess &&
             h->d_screen.alloc(tt) == cudaSuccess && h->d_sq.alloc(tt) == cudaSuccess &&
             h->d_sqf.alloc(tt) == cudaSuccess && h->d_dPf.alloc(nn) == cudaSuccess &&
-            h->d_Dsh.alloc(ss) == cudaSuccess && h->d_counters.alloc(3 * MMDG_NCLASS) == cudaSuccess;
+            h->d_Dsh.alloc(ss) == cudaSuccess && h->d_counters.alloc(kCounters * MMDG_NCLASS) == cudaSuccess;
   if (!ok) return fail(MMDG_E_NOMEM, "mmdg_set_basis: device allocation failed");
   // ---- primitive pairs
   {
@@ -1019,7 +1019,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   cudaStream_t st = (cudaStream_t)stream;
   const long long nn = h->ntot_nn;
   CUDA_TRY(cudaMemsetAsync(G, 0, sizeof(double) * nn, st));
-  CUDA_TRY(cudaMemsetAsync(h->d_counters.p, 0, sizeof(unsigned long long) * 3 * MMDG_NCLASS, st));
+  CUDA_TRY(cudaMemsetAsync(h->d_counters.p, 0, sizeof(unsigned long long) * kCounters * MMDG_NCLASS, st));
   k_prep_density<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(dP, h->d_dPf.p, nn);
   CUDA_TRY(cudaGetLastError());
   {
@@ -1115,7 +1115,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   ci = 0;
   for (const ClassEntry& e : kClasses) {
     const int cb = pair_class(e.la, e.lb), ck = pair_class(e.lc, e.ld);
-    f.counters = h->d_counters.p + 3 * ci;
+    f.counters = h->d_counters.p + kCounters * ci;
     cudaStream_t cs = ns > 1 ? h->side[ci % ns] : st;
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci], st));
     if (h->cls_count[cb] && h->cls_count[ck]) {
@@ -1142,7 +1142,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     for (int k = 0; k < 2 * MMDG_NCLASS; ++k) cudaEventDestroy(ev[k]);
   }
   if (counts) {
-    CUDA_TRY(cudaMemcpyAsync(counts, h->d_counters.p, sizeof(unsigned long long) * 3 * MMDG_NCLASS,
+    CUDA_TRY(cudaMemcpyAsync(counts, h->d_counters.p, sizeof(unsigned long long) * kCounters * MMDG_NCLASS,
                              cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
   }

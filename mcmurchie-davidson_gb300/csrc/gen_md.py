@@ -320,7 +320,61 @@ def gen_class_compact(la, lb, lc, ld):
     return "\n".join(o)
 
 
-# classes with la+lb+lc+ld above this use the compact form
+def _pair_records(la, lb):
+    """Packed records of the function pairs of (la lb), sorted by their number of
+    Hermite terms: real index | n_tau << 8 | n_nu << 12 | n_phi << 16 | E' offset << 20."""
+    terms, _ = pair_terms(la, lb)
+    recs = []
+    for idx, (a, b) in enumerate((a, b) for a in comps(la) for b in comps(lb)):
+        nt, nu, nph = a[0] + b[0] + 1, a[1] + b[1] + 1, a[2] + b[2] + 1
+        off = terms[idx][0][1]
+        assert len(terms[idx]) == nt * nu * nph and off < 4096
+        recs.append((nt * nu * nph, idx | nt << 8 | nu << 12 | nph << 16 | off << 20))
+    recs.sort(key=lambda r: r[0])
+    return [r[1] for r in recs]
+
+
+def gen_class_warp(la, lb, lc, ld):
+    """Tables and constants of the warp-cooperative Fock kernel (md_warp.cuh) of one
+    high-L class: function pairs sorted by Hermite term count."""
+    Lp, Lq = la + lb, lc + ld
+    L = Lp + Lq
+    s = f"{la}{lb}{lc}{ld}"
+    kab = _pair_records(la, lb)
+    kcd = _pair_records(lc, ld)
+    _, nnz_ab = pair_terms(la, lb)
+    _, nnz_cd = pair_terms(lc, ld)
+    o = []
+    o.append(f"static __constant__ unsigned kWB_{s}[{len(kab)}] = {{{', '.join(f'{x}u' for x in kab)}}};")
+    o.append(f"static __constant__ unsigned kWK_{s}[{len(kcd)}] = {{{', '.join(f'{x}u' for x in kcd)}}};")
+    o.append(f"template <typename Real>")
+    o.append(f"struct MDW_{s} {{")
+    o.append(f"  static constexpr int LA = {la}, LB = {lb}, LC = {lc}, LD = {ld}, L = {L};")
+    o.append(f"  static constexpr int NAB = {len(kab)}, NCD = {len(kcd)}, NNZ_AB = {nnz_ab}, NNZ_CD = {nnz_cd};")
+    o.append(f"  static constexpr int HL = {H(L)}, HP = {H(Lp)};")
+    o.append(f"  static __device__ __forceinline__ unsigned bra_pair(int x) {{ return kWB_{s}[x]; }}")
+    o.append(f"  static __device__ __forceinline__ unsigned ket_pair(int x) {{ return kWK_{s}[x]; }}")
+    o.append(f"  static __device__ __forceinline__ short herm(int x) {{ return kWH_{L}[x]; }}")
+    o.append(f"}};")
+    return "\n".join(o)
+
+
+def gen_herm_tables():
+    """Packed (t | u << 5 | v << 10) of every Hermite index, for each total L of the
+    warp-cooperative classes."""
+    out = []
+    for L in sorted({sum(c) for c in classes() if sum(c) > COMPACT_ABOVE_L}):
+        vals = [t | u << 5 | v << 10 for (t, u, v) in herm(L)]
+        out.append(f"static __constant__ short kWH_{L}[{len(vals)}] = {{{', '.join(map(str, vals))}}};")
+    return "\n".join(out)
+
+
+def is_warp_class(cl):
+    return sum(cl) > COMPACT_ABOVE_L
+
+
+# classes with la+lb+lc+ld above this use the compact form (and, for Fock builds,
+# the warp-cooperative kernel of md_warp.cuh)
 COMPACT_ABOVE_L = 4
 # register-resident classes up to this total L unroll the ket primitive loop by two
 UNROLL_KET_MAX_L = 2
@@ -333,6 +387,11 @@ def generate(path, overrides=None):
         ch, sm = overrides.get(cl, (None, None))
         parts.append(gen_class(*cl, chunk=ch, smem=sm))
         parts.append("")
+    parts.append(gen_herm_tables())
+    for cl in classes():
+        if is_warp_class(cl):
+            parts.append(gen_class_warp(*cl))
+            parts.append("")
     # class table for the host: smem doubles per thread
     parts.append("#define MMDG_FOR_EACH_CLASS(X) \\")
     cls = classes()
@@ -361,7 +420,8 @@ def generate_instances(outdir, ngroups=6):
         groups[k].append(c)
         load[k] += sz
     files = []
-    decl = ["// Generated by gen_md.py -- do not edit.", "#pragma once", '#include "md_kernels.cuh"', "namespace mmdg {",
+    decl = ["// Generated by gen_md.py -- do not edit.", "#pragma once", '#include "md_kernels.cuh"',
+            '#include "md_warp.cuh"', "namespace mmdg {",
             "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
@@ -393,8 +453,15 @@ def generate_instances(outdir, ngroups=6):
             s = "".join(map(str, c))
             md = f"MD_{s}"
             t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, const long long* koff, int nkeys, int grid, cudaStream_t st) {{")
-            t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>(), grid), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count, koff, nkeys);")
-            t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>(), grid), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count, koff, nkeys);")
+            if is_warp_class(c):
+                mw = f"MDW_{s}"
+                for real, cond in (("float", "if (prec)"), ("double", "else")):
+                    k = f"k_fock_warp<{mw}<{real}>, {real}>"
+                    sm = f"WarpSmem<{mw}<{real}>, {real}>::bytes()"
+                    t.append(f"  {cond} {k}<<<persistent_blocks({k}, {sm}, grid), kThreads, {sm}, st>>>(g, f, cl, list, count, koff, nkeys);")
+            else:
+                t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>(), grid), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count, koff, nkeys);")
+                t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>(), grid), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count, koff, nkeys);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_tensor_{s}(const Geometry& g, const TensorArgs& a, const ClassLaunch& cl, cudaStream_t st) {{")
@@ -407,8 +474,13 @@ def generate_instances(outdir, ngroups=6):
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_quartets<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
-            inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<double>, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
-            inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<float>, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<float>, float>()))) return e;")
+            if is_warp_class(c):
+                for real in ("double", "float"):
+                    mw = f"MDW_{s}<{real}>"
+                    inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock_warp<{mw}, {real}>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WarpSmem<{mw}, {real}>::bytes()))) return e;")
+            else:
+                inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<double>, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
+                inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<float>, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<float>, float>()))) return e;")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_tensor<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             if c[:2] == c[2:]:
                 t.append(f"cudaError_t launch_schwarz_{s}(const Geometry& g, const SchwarzArgs& a, const int* list, int n, cudaStream_t st) {{")

@@ -162,6 +162,7 @@ template <>
 struct Ctx<double> {
   const Geometry* g;
   int chunk;  // ket chunk evaluated by this thread, -1 = all chunks
+  mutable unsigned nasym;  // Boys evaluations on the asymptotic branch (counters)
   int bra_begin, bra_end, ket_begin, ket_end;
   long long ebra, eket;
   int nnz_ab, nnz_cd;
@@ -193,7 +194,9 @@ struct Ctx<double> {
     const double rsum = rsqrt(a.x + b.x);
     const double alpha = a.x * b.x * (rsum * rsum);
     double F[L + 1];
-    boys_eval<L>(g->boys64, alpha * r2, F);
+    const double T = alpha * r2;
+    nasym += T >= kBoysTaylorMax ? 1u : 0u;
+    boys_eval<L>(g->boys64, T, F);
     double c = kTwoPi52 * rsum;
     const double m2a = -2.0 * alpha;
 #pragma unroll
@@ -208,6 +211,7 @@ template <>
 struct Ctx<float> {
   const Geometry* g;
   int chunk;
+  mutable unsigned nasym;
   int bra_begin, bra_end, ket_begin, ket_end;
   long long ebra, eket;
   int nnz_ab, nnz_cd;
@@ -245,7 +249,9 @@ struct Ctx<float> {
     const float rsum = rsqrtf(pa + pb);
     const float alpha = pa * pb * (rsum * rsum);
     float F[L + 1];
-    boys_eval<L>(g->boys32, alpha * r2, F);
+    const float T = alpha * r2;
+    nasym += T >= float(kBoysTaylorMax) ? 1u : 0u;
+    boys_eval<L>(g->boys32, T, F);
     float c = float(kTwoPi52) * rsum;
     const float m2a = -2.0f * alpha;
 #pragma unroll
@@ -279,6 +285,11 @@ __device__ __forceinline__ float abs_f32_trunc(double x) {
 }
 
 // Fock (formPT) digest --------------------------------------------------------------
+// per-class counters of a Fock build: [0] digested function quartets, [1] shell
+// quartets, [2] primitive quartets, [3] bra-primitive passes (bra transforms),
+// [4] primitive quartets whose Boys function took the asymptotic branch (T >= 48)
+constexpr int kCounters = 5;
+
 struct FockArgs {
   const double* dP;      // packed per-molecule N x N (density difference)
   const float* dPf;      // FP32 copy of |dP| for screening
@@ -288,7 +299,7 @@ struct FockArgs {
   const float* Dsh;      // per-molecule S x S shell-block max |dP|
   double tol;
   float tolf_lo, tolf_hi;  // FP32 guard band around tol
-  unsigned long long* counters;  // [0] computed function quartets, [1] computed shell quartets
+  unsigned long long* counters;  // per class, kCounters entries (see kCounters)
   // sharded build (mmdg_set_partition): a shell quartet is kept only if the owner of
   // its pair with the larger canonical index is `part` (pair_owner null: no sharding)
   const int* pair_owner;  // per shell pair

@@ -33,6 +33,7 @@ __device__ __forceinline__ Ctx<Real> make_ctx(const Geometry& g, int bp, int kp,
   Ctx<Real> c;
   c.g = &g;
   c.chunk = -1;
+  c.nasym = 0;
   c.bra_begin = __ldg(g.pr_begin + bp);
   c.bra_end = c.bra_begin + __ldg(g.pr_count + bp);
   c.ket_begin = __ldg(g.pr_begin + kp);
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
   const long long total = (long long)n * MD::NCHUNK;
   extern __shared__ double smem_d[];
   Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
-  unsigned nfq = 0, nsq = 0, npq = 0;
+  unsigned nfq = 0, nsq = 0, npq = 0, nbp = 0, nas = 0;
   int key = 0;
   for (long long idx = blockIdx.x * (long long)kThreads + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * kThreads) {
@@ -167,16 +168,21 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
     if (chunk == 0) {
       ++nsq;
       npq += unsigned((c.bra_end - c.bra_begin) * (c.ket_end - c.ket_begin));
+      nbp += unsigned(c.bra_end - c.bra_begin);
+      nas += c.nasym;
     }
   }
   if (f.counters) {
     const unsigned mask = __activemask();
     const unsigned s0 = __reduce_add_sync(mask, nfq), s1 = __reduce_add_sync(mask, nsq),
-                   s2 = __reduce_add_sync(mask, npq);
+                   s2 = __reduce_add_sync(mask, npq), s3 = __reduce_add_sync(mask, nbp),
+                   s4 = __reduce_add_sync(mask, nas);
     if ((threadIdx.x & 31) == __ffs(mask) - 1 && (s0 | s1 | s2)) {
       atomicAdd(f.counters + 0, (unsigned long long)s0);
       atomicAdd(f.counters + 1, (unsigned long long)s1);
       atomicAdd(f.counters + 2, (unsigned long long)s2);
+      atomicAdd(f.counters + 3, (unsigned long long)s3);
+      atomicAdd(f.counters + 4, (unsigned long long)s4);
     }
   }
 }

@@ -15,6 +15,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmmdg.so")
 NCLASS = 21
+NCOUNT = 5  # per-class counters of a Fock build (mmdg_fock)
 DEFAULT_STREAMS_SINGLE = 4
 MAX_COMP = 6
 LMAX = 2
@@ -52,6 +53,7 @@ def _bind(L):
         "mmdg_eri_quartets": (c_int, [p, c_ll, p, p, p]),
         "mmdg_set_partition": (c_int, [p, c_int, c_int, p, c_ll]),
         "mmdg_device_bytes": (c_int, [p, ctypes.POINTER(c_ll)]),
+        "mmdg_ao2mo": (c_int, [c_ll, p, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -233,23 +235,23 @@ class Context:
             raise ValueError("dP must be a contiguous CUDA float64 tensor of sum N_m^2 elements")
         if G is None:
             G = torch.empty_like(dP)
-        cnt = np.zeros(3 * NCLASS, dtype=np.uint64) if counts else None
+        cnt = np.zeros(NCOUNT * NCLASS, dtype=np.uint64) if counts else None
         check(lib().mmdg_fock(self._h, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(G.data_ptr()), float(tol),
                               float(fp32_below), _ptr(cnt) if counts else None, stream_ptr()), "mmdg_fock")
         if counts:
-            self.last_counts = cnt.reshape(NCLASS, 3)
+            self.last_counts = cnt.reshape(NCLASS, NCOUNT)
         return G
 
     def fock_timed(self, dP, G=None, tol: float = 1e-12, fp32_below: float = 0.0):
         """As ``fock`` with per-class device times (ms) and counts: returns (G, class_ms, counts)."""
         if G is None:
             G = self.torch.empty_like(dP)
-        cnt = np.zeros(3 * NCLASS, dtype=np.uint64)
+        cnt = np.zeros(NCOUNT * NCLASS, dtype=np.uint64)
         ms = np.zeros(NCLASS, dtype=np.float32)
         check(lib().mmdg_fock_timed(self._h, ctypes.c_void_p(dP.data_ptr()), ctypes.c_void_p(G.data_ptr()),
                                     float(tol), float(fp32_below), _ptr(cnt), _ptr(ms), stream_ptr()),
               "mmdg_fock_timed")
-        self.last_counts = cnt.reshape(NCLASS, 3)
+        self.last_counts = cnt.reshape(NCLASS, NCOUNT)
         return G, ms, self.last_counts
 
     def fock_update(self, G, F_in, F_out):
@@ -298,3 +300,20 @@ def scratch_context():
         b.jk_dense = lambda T, P, J, K: Context.jk_dense(b, T, P, J, K)
         _default_ctx = b
     return _default_ctx
+
+
+def ao2mo(C, eri, out=None, work=None):
+    """(PQ|RS) = sum C[p,P] C[q,Q] C[r,R] C[s,S] (pq|rs) on the device (mmdg_ao2mo):
+    ``C`` (N x N) and ``eri`` (N^4) are CUDA float64 tensors; returns ``out``."""
+    torch = _torch()
+    N = int(C.shape[0])
+    if C.dtype != torch.float64 or eri.dtype != torch.float64 or eri.numel() != N ** 4:
+        raise ValueError("ao2mo: float64 C (N x N) and ERI tensor (N^4) expected")
+    C = C.contiguous()
+    eri = eri.contiguous()
+    out = torch.empty_like(eri) if out is None else out
+    work = torch.empty_like(eri) if work is None else work
+    check(lib().mmdg_ao2mo(N, ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(eri.data_ptr()),
+                           ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(work.data_ptr()), stream_ptr()),
+          "mmdg_ao2mo")
+    return out

@@ -88,3 +88,122 @@ def build_flops(counts, kind: str = "model") -> float:
         else:
             tot += executed_flops_per_prim_quartet(*cls) * npq + 12.0 * nfq
     return tot
+
+
+# ------------------------------------------------------------------ issued / useful FP64 FLOPs
+# What the Fock kernels really issue, counted from the structure of the generated
+# code (csrc/gen_md.py, csrc/md_device.cuh, csrc/md_warp.cuh), lane by lane, with an
+# FMA as 2 FLOPs and a multiply or add as 1 -- the quantity that ncu's
+# smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on counters measure as
+# 2 DFMA + DMUL + DADD.  Not counted: the FP64 instructions inside CUDA's rsqrt and
+# exp (library code, called as such), conversions and compares (the ncu summary
+# gives their share).  Per-class inputs are the Fock build's counters: digested
+# function quartets, shell quartets, primitive quartets, bra-primitive passes and
+# asymptotic-branch Boys evaluations.
+
+def _gen_md():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "csrc", "gen_md.py")
+    spec = importlib.util.spec_from_file_location("_gen_md_for_flops", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@lru_cache(maxsize=None)
+def _gm():
+    return _gen_md()
+
+
+def boys_flops(L: int, asymptotic: bool) -> int:
+    """boys_eval<L> (md_device.cuh): Taylor row + exp row + downward recursion, or
+    the asymptotic start F_0 and upward recursion (T >= 48)."""
+    if not asymptotic:
+        return 17 + (15 + 3 * L if L > 0 else 0)
+    if L == 0:
+        return 1
+    return 2 + (1 + 3 * L if L > 4 else 2 * L)
+
+
+def r0_flops(L: int, asymptotic: bool) -> int:
+    """hermite_r0_pp<L>: P - Q, |PQ|^2, p + q, alpha, T, Boys, prefactor powers."""
+    return 3 + 5 + 1 + 3 + 1 + boys_flops(L, asymptotic) + 2 + (2 * L + 1)
+
+
+@lru_cache(maxsize=None)
+def recursion_flops(L: int) -> int:
+    """The in-place Hermite Coulomb recursion of the per-thread code: X R1 (1 FLOP), or
+    fma(X, R1, (m-1) R2) (3 FLOPs) when the stepped index m exceeds 1."""
+    g = _gm()
+    tot = 0
+    for s in range(1, L + 1):
+        for (t, u, v) in g.herm(s):
+            if (t, u, v) == (0, 0, 0):
+                continue
+            m = t if t > 0 else (u if u > 0 else v)
+            tot += 3 if m > 1 else 1
+    return tot
+
+
+@lru_cache(maxsize=None)
+def _thread_config(cls):
+    """(chunk passes, ket FLOPs per primitive quartet, bra FLOPs per bra pass) of the
+    per-thread Fock kernel of a class."""
+    g = _gm()
+    la, lb, lc, ld = cls
+    chunk, _ = g.choose(la, lb, lc, ld)
+    ncd = C(lc) * C(ld)
+    nch = -(-ncd // chunk)
+    hp = H(la + lb)
+    return nch, 2 * hp * nnz(lc, ld), 2 * nnz(la, lb) * ncd
+
+
+@lru_cache(maxsize=None)
+def _warp_config(cls):
+    """(ket FLOPs per primitive quartet, bra FLOPs per bra pass, R-level FLOPs) issued by
+    the warp-cooperative kernel: every lane of a pass runs the pass's longest term loop."""
+    g = _gm()
+    la, lb, lc, ld = cls
+    L, hp = la + lb + lc + ld, H(la + lb)
+    kcd = [((r >> 8) & 15) * ((r >> 12) & 15) * ((r >> 16) & 15) for r in g._pair_records(lc, ld)]
+    kab = [((r >> 8) & 15) * ((r >> 12) & 15) * ((r >> 16) & 15) for r in g._pair_records(la, lb)]
+    ncd, nab = len(kcd), len(kab)
+    ket = 0
+    for m in range(-(-ncd * hp // 32)):
+        ket += max(kcd[o // hp] for o in range(32 * m, min(32 * m + 32, ncd * hp)))
+    bra = 0
+    for m in range(-(-nab * ncd // 32)):
+        bra += max(kab[o // ncd] for o in range(32 * m, min(32 * m + 32, nab * ncd)))
+    rlev = 3 * sum(H(s) for s in range(1, L + 1))
+    return 64 * ket, 64 * bra, rlev
+
+
+def fock_kernel(cls) -> str:
+    return "warp" if _gm().is_warp_class(tuple(cls)) else "thread"
+
+
+def issued_flops(cls, row) -> float:
+    """FP64 FLOPs the Fock kernel of class ``cls`` issues for the counters ``row``."""
+    nfq, nsq, npq, nbp, nas = (float(x) for x in list(row) + [0.0] * (5 - len(row)))
+    L = sum(cls)
+    r0 = (npq - nas) * r0_flops(L, False) + nas * r0_flops(L, True)
+    if fock_kernel(cls) == "warp":
+        ket, bra, rlev = _warp_config(tuple(cls))
+        return r0 + npq * (rlev + ket) + nbp * bra + 6.0 * nfq
+    nch, ket, bra = _thread_config(tuple(cls))
+    return nch * (r0 + npq * recursion_flops(L)) + npq * ket + nbp * bra + 6.0 * nfq
+
+
+def useful_flops(cls, row) -> float:
+    """The algorithm's own FP64 FLOPs for the counters ``row``: Boys and R once per
+    primitive quartet, the ket transform over the non-zero Hermite terms once per
+    primitive quartet, the bra transform once per bra primitive, six products per
+    digested function quartet -- no recomputation, no padded lanes."""
+    nfq, nsq, npq, nbp, nas = (float(x) for x in list(row) + [0.0] * (5 - len(row)))
+    la, lb, lc, ld = cls
+    L = la + lb + lc + ld
+    r0 = (npq - nas) * r0_flops(L, False) + nas * r0_flops(L, True)
+    ket = 2 * H(la + lb) * nnz(lc, ld)
+    bra = 2 * nnz(la, lb) * C(lc) * C(ld)
+    return r0 + npq * (recursion_flops(L) + ket) + nbp * bra + 6.0 * nfq

@@ -2,8 +2,8 @@
 ``mmd.postscf.PostSCF`` API (mmd/postscf.py:13-73).
 
 ``PostSCF(mol)`` requires a converged conventional RHF (the device ERI tensor) and
-runs ``ao2mo``: the 4-index transform (pq|rs) -> (PQ|RS) as four FP64 contractions
-over one index each (cuBLAS DGEMMs through torch: plain library GEMMs), the
+runs ``ao2mo``: the 4-index transform (pq|rs) -> (PQ|RS) as four FP64 quarter
+transforms over one index each (the project's kernel, mmdg_ao2mo), the
 spin-orbital antisymmetrised integrals <AB||CD> (spin orbital 2p + sigma, the
 ordering of the reference's Kronecker products; built on first use), the spin-orbital
 core Hamiltonian ``Hp`` and orbital energies ``fs`` -- the attributes the reference
@@ -25,6 +25,8 @@ import sys
 
 import numpy as np
 
+from . import _native
+
 
 class PostSCF:
     """Post-SCF methods on a converged RHF molecule (mmd/postscf.py:13-19)."""
@@ -44,15 +46,9 @@ class PostSCF:
         dev = mol._dev["S"].device
         N = mol.nbasis
         C = torch.as_tensor(np.real(np.asarray(mol.C)), dtype=torch.float64, device=dev)
-        T = mol._dev["TwoE"]
-        # one index at a time: s, r, q, p (each a (N^3 x N) @ (N x N) GEMM)
-        T = (T.reshape(N ** 3, N) @ C).reshape(N, N, N, N)                                 # pqrS
-        T = (T.permute(0, 1, 3, 2).reshape(N ** 3, N) @ C).reshape(N, N, N, N)            # pqSR
-        T = T.permute(0, 1, 3, 2)                                                          # pqRS
-        T = (T.permute(0, 2, 3, 1).reshape(N ** 3, N) @ C).reshape(N, N, N, N)            # pRSQ
-        T = T.permute(0, 3, 1, 2)                                                          # pQRS
-        T = (T.permute(1, 2, 3, 0).reshape(N ** 3, N) @ C).reshape(N, N, N, N)            # QRSP
-        mo = T.permute(3, 0, 1, 2).contiguous()                                            # PQRS
+        # the four quarter transforms in libmmdg.so (mmdg_ao2mo): each contracts the
+        # last index and writes the new one first, pqrs -> Spqr -> RSpq -> QRSp -> PQRS
+        mo = _native.ao2mo(C, mol._dev["TwoE"].reshape(-1)).view(N, N, N, N)
         self._mo = mo
         mol.single_bar = mo.cpu().numpy()
         mol.norb = 2 * N

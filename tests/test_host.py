@@ -264,3 +264,24 @@ def test_save_integrals_writes_the_crawford_files(golden, tmp_path):
     assert (idx[:3] == [[0, 0, 0, 0], [0, 0, 0, 1], [0, 0, 0, 2]]).all()
     assert np.abs(rows[:, 4] - d["TwoE"][idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3]]).max() < 1e-15
     assert open(out + "/geometry.txt").read().strip() == str(d["geometry"]).strip()
+
+
+def test_issued_and_useful_flop_counts():
+    """The issued-FLOP count mirrors the code: one chunk pass and no padding equals
+    the useful count; chunked classes and the warp kernel's padded lanes issue more;
+    the Boys branch matters; (ss|ss) is counted by hand."""
+    from mmd import flop_model as F
+    row = [100.0, 10.0, 50.0, 20.0, 10.0]  # fq, shell q., prim q., bra passes, asymptotic Boys
+    for c in F.CLASSES:
+        i, u = F.issued_flops(c, row), F.useful_flops(c, row)
+        assert i >= u > 0
+        if F.fock_kernel(c) == "thread" and F._thread_config(tuple(c))[0] == 1:
+            assert i == u
+    assert F.fock_kernel((2, 2, 2, 2)) == "warp" and F.fock_kernel((1, 0, 0, 0)) == "thread"
+    # (ss|ss), Taylor branch: P-Q 3, |PQ|^2 5, p+q 1, alpha 3, T 1, Boys 17, prefactor 2 + 1;
+    # ket 2 per primitive quartet, bra 2 per bra pass, 6 per digested function quartet
+    assert F.r0_flops(0, False) == 3 + 5 + 1 + 3 + 1 + 17 + 2 + 1
+    assert F.useful_flops((0, 0, 0, 0), [1, 1, 1, 1, 0]) == F.r0_flops(0, False) + 2 + 2 + 6
+    assert F.boys_flops(3, True) < F.boys_flops(3, False)
+    # the recursion counts 1 FLOP for a first step and 3 for fma(X, R1, (m-1) R2)
+    assert F.recursion_flops(1) == 3 and F.recursion_flops(2) == 3 + 6 * 1 + 3 * 3
