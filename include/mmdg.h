@@ -226,6 +226,11 @@ int mmdg_mlp_to_bf16(const float* w, void* w_bf16, long long n, void* stream);
  * transforms (each contracts the last index and writes the new one first). */
 int mmdg_ao2mo(long long N, const double* C, const double* eri_in, double* eri_out, double* work, void* stream);
 
+/* The ERI kernels' reciprocal square root (an FP32 estimate refined by one
+ * third-order FP64 step) and CUDA's rsqrt at n points, for x in the normal float
+ * range (device arrays).  Test support; no counterpart in the reference. */
+int mmdg_rsqrt(mmdg_context* ctx, long long n, const double* x, double* ours, double* cuda, void* stream);
+
 /* Boys function F_m(T) for integer 0 <= m <= 8 at n points (device arrays). */
 int mmdg_boys(mmdg_context* ctx, int m, long long n, const double* T, double* out, void* stream);
 

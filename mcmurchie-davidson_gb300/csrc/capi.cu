@@ -141,11 +141,13 @@ static void build_boys_table_raw(double* t64, float* t32) {
     dd F[mtop + 1];
     F[mtop] = dd_div_d(dd_mul(eT, sum), 2.0 * mtop + 1.0);
     for (int m = mtop; m > 0; --m) F[m - 1] = dd_div_d(dd_add(dd_mul_d(F[m], 2.0 * T), eT), 2.0 * m - 1.0);
-    for (int L = 0; L <= kBoysLMax; ++L)
+    for (int L = 0; L <= kBoysLMax; ++L) {
       for (int n = 0; n < 7; ++n) {
         const dd v = dd_div_d(F[L + n], fact[n]);
         t64[(L * kBoysNGrid + k) * kBoysRow + n] = v.hi + v.lo;
       }
+      t64[(L * kBoysNGrid + k) * kBoysRow + 7] = T;  // the grid point, exact (k/16)
+    }
     for (int n = 0; n < 8; ++n) {
       const dd v = dd_div_d(eT, fact[n]);
       t64[kBoysExpOff + k * kBoysRow + n] = v.hi + v.lo;
@@ -412,7 +414,9 @@ __global__ void k_build_pairs(PairBuildArgs a) {
         for (int xb = lb; xb >= 0; --xb)
           for (int yb = lb - xb; yb >= 0; --yb) {
             const int zb = lb - xb - yb;
-            const double c = K * na * comp_norm(xb) * comp_norm(yb) * comp_norm(zb);
+            // sqrt(2 pi^{5/2}) per coefficient: a bra-ket product carries the
+            // primitive ERI's 2 pi^{5/2} (cython/twoe.pyx:93)
+            const double c = kSqrtTwoPi52 * K * na * comp_norm(xb) * comp_norm(yb) * comp_norm(zb);
             for (int t = 0; t <= xa + xb; ++t)
               for (int u = 0; u <= ya + yb; ++u)
                 for (int v = 0; v <= za + zb; ++v) {
@@ -1206,6 +1210,24 @@ extern "C" int mmdg_boys(mmdg_context* h, int m, long long n, const double* T, d
     case 7: k_boys<7><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
     default: k_boys<8><<<nb, 256, 0, st>>>(h->boys64.p, T, out, n); break;
   }
+  CUDA_TRY(cudaGetLastError());
+  return MMDG_OK;
+}
+
+// 1/sqrt(x) of the ERI kernels (rsqrt_dd: FP32 estimate + one third-order FP64 step)
+// and CUDA's rsqrt side by side, for the accuracy test
+__global__ void k_rsqrt(const double* x, double* ours, double* cuda, long long n) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ours[i] = rsqrt_dd(x[i]);
+  cuda[i] = rsqrt(x[i]);
+}
+
+extern "C" int mmdg_rsqrt(mmdg_context* h, long long n, const double* x, double* ours, double* cuda, void* stream) {
+  if (!h || (n > 0 && (!x || !ours || !cuda))) return fail(MMDG_E_ARG, "mmdg_rsqrt: null argument");
+  if (n <= 0) return MMDG_OK;
+  DeviceGuard dg(h->device);
+  k_rsqrt<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, ours, cuda, n);
   CUDA_TRY(cudaGetLastError());
   return MMDG_OK;
 }

@@ -28,7 +28,40 @@ constexpr int kBoysExpOff = kBoysNGrid * (kBoysLMax + 1) * kBoysRow;  // exp row
 constexpr int kBoysTabSize = kBoysExpOff + kBoysNGrid * kBoysRow;
 constexpr double kBoysTaylorMax = 48.0 - 1.0 / 32.0;
 constexpr double kTwoPi52 = 34.986836655249725;  // 2 pi^{5/2}
+// sqrt(2 pi^{5/2}): folded into every E' coefficient by the pair kernel, so the
+// product of a bra and a ket coefficient carries the 2 pi^{5/2} of the primitive ERI
+// (cython/twoe.pyx:93) and the quartet code multiplies by 1/sqrt(p+q) only
+constexpr double kSqrtTwoPi52 = 5.9149671727955846;
 constexpr double kHalfSqrtPi = 0.88622692545275801;
+
+// A non-negative double as a float rounded toward zero, from its bit pattern on the
+// integer pipe (exponent rebiased, top 23 mantissa bits kept: relative error below
+// 2^-23); values below the normal float range (zero included) give 0.
+__device__ __forceinline__ float f32_of_nonneg(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int fe = min((hi >> 20) - (1023 - 127), 254);
+  return fe <= 0 ? 0.0f : __int_as_float((fe << 23) | ((hi & 0xfffff) << 3) | (int)(lo >> 29));
+}
+
+// a positive normal float as a double, exactly, on the integer pipe
+__device__ __forceinline__ double f64_of_positive(float y) {
+  const int b = __float_as_int(y);
+  return __hiloint2double((((b >> 23) + (1023 - 127)) << 20) | ((b & 0x7fffff) >> 3), (b & 7) << 29);
+}
+
+// 1/sqrt(x) for a positive double whose magnitude is within the normal float range:
+// the single-precision estimate y0 = rsqrtf(x) (special-function unit; x and y0
+// moved between formats on the integer pipe) and one third-order step of the
+// Newton/Householder iteration for the inverse square root,
+//     e = 1 - x y0^2,   y = y0 (1 + e/2 + 3 e^2/8),
+// whose error is 5/16 e^3 + O(e^4); |e| < 2^-20 leaves it far below double rounding.
+// Five FP64 instructions.
+__device__ __forceinline__ double rsqrt_dd(double x) {
+  const double y0 = f64_of_positive(rsqrtf(f32_of_nonneg(x)));
+  const double e = fma(-x, y0 * y0, 1.0);  // y0 has 24 significant bits: y0^2 is exact
+  return fma(y0, e * fma(e, 0.375, 0.5), y0);
+}
 
 // ---------------------------------------------------------------------------------
 // geometry shared by every kernel
@@ -67,26 +100,36 @@ struct Geometry {
 //   F_L(T) = sum_n c_n y^n,  y = T_k - T,  |y| <= 1/32,
 // and row (k, exp) holds e_n = exp(-T_k) / n!, n = 0..7, for exp(-T) = sum_n e_n y^n.
 // Truncation: F_{L+7} |y|^7 / 7! < 6e-15 F_L and |y|^8/8! < 3e-17 relative.
+// Horner evaluation of one Taylor row c_0..c_6 at y (six FMAs)
+__device__ __forceinline__ double boys_row(const double2& c01, const double2& c23, const double2& c45, const double2& c67,
+                                           double y) {
+  double f = fma(c67.x, y, c45.y);
+  f = fma(f, y, c45.x);
+  f = fma(f, y, c23.y);
+  f = fma(f, y, c23.x);
+  f = fma(f, y, c01.y);
+  return fma(f, y, c01.x);
+}
+
+// The table index k = round(16 T) and the branch test come from an FP32 copy of T
+// (integer and FP32 pipes); slot 7 of every F row holds T_k itself, so y = T_k - T is
+// one FP64 subtraction.  T_f <= T (truncated toward zero), so |y| stays within
+// 1/32 + 2^-17.
 template <int L>
 __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double T, double* Fn) {
-  if (T < kBoysTaylorMax) {
-    // k = round(16 T) without FP64<->int conversions (which issue on the FP64 pipe):
-    // adding 1.5 * 2^52 leaves round(16 T) in the low mantissa bits (0 <= 16 T < 767.5)
-    constexpr double kRound = 6755399441055744.0;
-    const double r = fma(T, 16.0, kRound);
-    const int k = __double2loint(r);
-    const double y = fma(r - kRound, 0.0625, -T);  // T_k - T
-    // a table row is 64 bytes (64-byte aligned): four 16-byte loads instead of seven
-    // or eight 8-byte ones relieve the L1/texture path
+  const float Tf = f32_of_nonneg(T);
+  if (Tf < float(kBoysTaylorMax)) {
+    const int k = __float2int_rn(Tf * 16.0f);
+    // a table row is 64 bytes (64-byte aligned): four 16-byte loads
     const double2* __restrict__ c = reinterpret_cast<const double2*>(tab + (L * kBoysNGrid + k) * kBoysRow);
     const double2 c01 = __ldg(c), c23 = __ldg(c + 1), c45 = __ldg(c + 2), c67 = __ldg(c + 3);
-    double f = fma(c67.x, y, c45.y);
-    f = fma(f, y, c45.x);
-    f = fma(f, y, c23.y);
-    f = fma(f, y, c23.x);
-    f = fma(f, y, c01.y);
-    Fn[L] = fma(f, y, c01.x);
-    if (L > 0) {
+    const double y = c67.y - T;  // T_k - T
+    Fn[L] = boys_row(c01, c23, c45, c67, y);
+    if (L == 1) {
+      // F_0 from its own row: 6 FMAs instead of exp(-T) (7) and one recursion step (3)
+      const double2* __restrict__ c0 = reinterpret_cast<const double2*>(tab + k * kBoysRow);
+      Fn[0] = boys_row(__ldg(c0), __ldg(c0 + 1), __ldg(c0 + 2), __ldg(c0 + 3), y);
+    } else if (L > 1) {
       const double2* __restrict__ e = reinterpret_cast<const double2*>(tab + kBoysExpOff + k * kBoysRow);
       const double2 e01 = __ldg(e), e23 = __ldg(e + 1), e45 = __ldg(e + 2), e67 = __ldg(e + 3);
       double x = fma(e67.y, y, e67.x);
@@ -103,7 +146,7 @@ __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double
   } else {
     // F_0 = sqrt(pi/T)/2 and F_{m+1} = ((2m+1) F_m - exp(-T)) / (2T); for T >= 48 and
     // m <= 4 the exp(-T) terms change F_m by less than 5e-15 relative and are dropped
-    const double rs = rsqrt(T);
+    const double rs = rsqrt_dd(T);
     Fn[0] = kHalfSqrtPi * rs;
     if (L > 0) {
       const double iT = rs * rs;
@@ -191,13 +234,13 @@ struct Ctx<double> {
     Y = a.z - b.z;
     Z = a.w - b.w;
     const double r2 = fma(X, X, fma(Y, Y, Z * Z));
-    const double rsum = rsqrt(a.x + b.x);
+    const double rsum = rsqrt_dd(a.x + b.x);
     const double alpha = a.x * b.x * (rsum * rsum);
     double F[L + 1];
     const double T = alpha * r2;
-    nasym += T >= kBoysTaylorMax ? 1u : 0u;
+    nasym += f32_of_nonneg(T) >= float(kBoysTaylorMax) ? 1u : 0u;
     boys_eval<L>(g->boys64, T, F);
-    double c = kTwoPi52 * rsum;
+    double c = rsum;  // 2 pi^{5/2} is folded into the E' coefficients
     const double m2a = -2.0 * alpha;
 #pragma unroll
     for (int n = 0; n <= L; ++n) {
@@ -252,7 +295,7 @@ struct Ctx<float> {
     const float T = alpha * r2;
     nasym += T >= float(kBoysTaylorMax) ? 1u : 0u;
     boys_eval<L>(g->boys32, T, F);
-    float c = float(kTwoPi52) * rsum;
+    float c = rsum;  // 2 pi^{5/2} is folded into the E' coefficients
     const float m2a = -2.0f * alpha;
 #pragma unroll
     for (int n = 0; n <= L; ++n) {

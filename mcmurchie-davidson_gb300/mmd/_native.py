@@ -54,6 +54,7 @@ def _bind(L):
         "mmdg_set_partition": (c_int, [p, c_int, c_int, p, c_ll]),
         "mmdg_device_bytes": (c_int, [p, ctypes.POINTER(c_ll)]),
         "mmdg_ao2mo": (c_int, [c_ll, p, p, p, p, p]),
+        "mmdg_rsqrt": (c_int, [p, c_ll, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -16,7 +16,7 @@
  * Here 1F1 is evaluated through Kummer's transformation
  *     1F1(a; b; -T) = exp(-T) 1F1(b-a; b; T),  b-a = 1,
  * i.e.  F_m(T) = exp(-T)/(2m+1) * sum_k T^k / ((m+3/2)(m+5/2)...(m+1/2+k)),
- * a series of positive terms (no cancellation), summed in long double; for
+ * a series of positive terms (no cancellation), summed in double-double; for
  * T > 200 (and m < T/4) the asymptotic value Gamma(m+1/2) / (2 T^(m+1/2)) is
  * used, whose relative error exp(-T) T^(m+1/2)/Gamma(m+1/2) is below 1e-60 there.
  * The pins are tests/test012.py:12-69 of the reference (50 literature values)
@@ -29,19 +29,66 @@
 #define ORACLE_PI 3.141592653589793238462643383279 /* cython/util.pxi:7 */
 
 /* ---------------------------------------------------------------- Boys */
+/* Double-double arithmetic (error-free transformations with fma): the series below
+ * is summed to ~1e-30 relative on every host -- x86 and Arm alike (on aarch64 a
+ * `long double` is software quad precision, far too slow for the bench-size checks). */
+typedef struct {
+  double hi, lo;
+} odd;
+static odd odd_two_sum(double a, double b) {
+  double s = a + b, bb = s - a;
+  odd r = {s, (a - (s - bb)) + (b - bb)};
+  return r;
+}
+static odd odd_quick(double a, double b) {
+  double s = a + b;
+  odd r = {s, b - (s - a)};
+  return r;
+}
+static odd odd_add(odd a, odd b) {
+  odd s = odd_two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return odd_quick(s.hi, s.lo);
+}
+static odd odd_mul_d(odd a, double b) {
+  double p = a.hi * b;
+  double e = fma(a.hi, b, -p) + a.lo * b;
+  return odd_quick(p, e);
+}
+static odd odd_div_d(odd a, double b) {
+  double q1 = a.hi / b;
+  odd r = odd_add(a, odd_mul_d((odd){q1, 0.0}, -b));
+  double q2 = r.hi / b;
+  return odd_quick(q1, q2);
+}
+
 double oracle_boys(double m, double T) {
+  const double mi = floor(m);
   if (T > 200.0 && m < T / 4.0) {
-    long double v = tgammal((long double)m + 0.5L) / (2.0L * powl((long double)T, (long double)m + 0.5L));
-    return (double)v;
+    /* Gamma(m+1/2) / (2 T^(m+1/2)); for integer m, Gamma(m+1/2) = sqrt(pi) prod_{k=1..m} (k-1/2) */
+    if (mi == m && m >= 0.0 && m < 200.0) {
+      odd g = {1.772453850905516, -7.666586499825799e-17}; /* sqrt(pi), double-double */
+      odd tp = {1.0, 0.0};
+      for (int k = 1; k <= (int)m; ++k) {
+        g = odd_mul_d(g, k - 0.5);
+        tp = odd_mul_d(tp, T);
+      }
+      const double st = sqrt(T);
+      return (g.hi + g.lo) / (2.0 * (tp.hi + tp.lo) * st);
+    }
+    return tgamma(m + 0.5) / (2.0 * pow(T, m + 0.5));
   }
-  long double term = 1.0L, sum = 1.0L, x = (long double)T;
-  long double b = (long double)m + 1.5L;
+  /* Kummer: F_m(T) = exp(-T)/(2m+1) * sum_k T^k / ((m+3/2)(m+5/2)...(m+1/2+k)) */
+  odd term = {1.0, 0.0}, sum = {1.0, 0.0};
+  const double b = m + 1.5;
   for (int k = 0; k < 100000; ++k) {
-    term *= x / (b + (long double)k);
-    sum += term;
-    if (term < sum * 1e-21L) break;
+    term = odd_div_d(odd_mul_d(term, T), b + (double)k);
+    sum = odd_add(sum, term);
+    if (term.hi < sum.hi * 1e-20) break;  /* far below the double result's rounding */
   }
-  return (double)(expl(-x) * sum / (2.0L * (long double)m + 1.0L));
+  /* exp(-T) correctly rounded to within an ulp by libm; the product and the division
+   * add two roundings: ~3e-16 relative overall */
+  return exp(-T) * (sum.hi + sum.lo) / (2.0 * m + 1.0);
 }
 
 /* ------------------------------------------- Hermite E (cython/util.pxi:13-28) */

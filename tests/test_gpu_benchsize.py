@@ -177,4 +177,5 @@ def test_eri_quartets_in_every_shell_order_match_the_tensor():
         fa, fb, fc, fd = (ss.func[s][ss.func[s] >= 0] for s in (a, b, c, e))
         ref = T[np.ix_(fa, fb, fc, fd)]
         assert np.abs(got[x, : len(fa), : len(fb), : len(fc), : len(fd)] - ref).max() < 1e-14
-    assert np.abs(T - d["TwoE"]).max() < 1e-12
+    idx = d["TwoE_idx"]  # the reference's own values of a sample of the tensor
+    assert np.abs(T[idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3]] - d["TwoE_val"]).max() < 1e-12

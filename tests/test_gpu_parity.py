@@ -43,6 +43,33 @@ def test_boys_gpu_vs_mpmath():
         assert rel.max() < 1e-14, (m, rel.max(), g["T"][rel.argmax()])
 
 
+def test_rsqrt_of_the_eri_kernels_within_one_ulp():
+    """rsqrt_dd (FP32 estimate + one third-order Newton/Householder step in FP64) is
+    within 1 ulp of the exact 1/sqrt(x) over the range the kernels use it on (p + q of
+    primitive pairs, and T >= 48 in the Boys function), like CUDA's own rsqrt."""
+    import ctypes
+    import torch
+    from mmd import _native
+    mp = pytest.importorskip("mpmath")
+    rng = np.random.default_rng(11)
+    x = np.concatenate([10.0 ** rng.uniform(-2, 9, 20000), rng.uniform(0.1, 100.0, 20000),
+                        np.array([1.0, 2.0, 3.0, 48.0, 47.96875, 1e-3, 123456.789])])
+    xd = torch.tensor(x, device="cuda")
+    ours, cuda = torch.empty_like(xd), torch.empty_like(xd)
+    ctx = _native.scratch_context()
+    _native.check(_native.lib().mmdg_rsqrt(ctx._h, xd.numel(), ctypes.c_void_p(xd.data_ptr()),
+                                           ctypes.c_void_p(ours.data_ptr()), ctypes.c_void_p(cuda.data_ptr()),
+                                           _native.stream_ptr()), "mmdg_rsqrt")
+    o, c = ours.cpu().numpy(), cuda.cpu().numpy()
+    mp.mp.dps = 40
+    sel = np.arange(0, len(x), 7)
+    exact = np.array([float(1 / mp.sqrt(mp.mpf(float(v)))) for v in x[sel]])
+    ulp = np.spacing(exact)
+    assert np.abs(o[sel] - exact).max() <= 1.0 * ulp.max() and np.all(np.abs(o[sel] - exact) <= ulp)
+    assert np.all(np.abs(c[sel] - exact) <= ulp)
+    assert np.all(np.abs(o - c) <= 2 * np.spacing(c))
+
+
 def test_boys_gpu_rejects_orders_outside_the_path():
     from mmd.integrals.onee import _boys
     with pytest.raises(ValueError):
