@@ -256,7 +256,7 @@ def run_cpu_sample(n_cand_target, n_surv_target, steps, warmup, cores=None):
 
 
 # ------------------------------------------------------------------------------ batched (config 3)
-def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3):
+def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3, parity_sample=128):
     """1024 seeded (H2O)n clusters, n ~ U{1..8}, 6-31G: one batched, graph-replayed and
     autotuned Fock launch for all molecules vs per-molecule launches, and the batched
     RHF to convergence."""
@@ -294,8 +294,17 @@ def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3):
                                          [P1h[i, :br.N[i], :br.N[i]] for i in idx])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    E = br.run(conver=1e-8)
+    E = br.run(conver=1e-8, polish=True)
     t_scf = time.perf_counter() - t0
+    # parity: a seeded random subset of the molecules through the single-molecule path
+    # (Molecule(...).RHF(direct=True), same convergence and polish) -- both energies
+    # are exact to second order in their densities' error
+    from mmd.molecule import Molecule
+    pick = np.sort(np.random.default_rng(4242).choice(nmol, size=min(parity_sample, nmol), replace=False))
+    dE = []
+    for i in pick:
+        e1 = Molecule(geoms[i], "6-31g").RHF(doPrint=False, direct=True, conver=1e-8, polish=True)
+        dE.append(abs(float(E[i]) - float(e1)))
     return {"molecules": nmol, "basis": "6-31G", "n_water": "U{1..8}", "nbasis_total": int(br.N.sum()),
             "batched_fock_builds_per_s": nmol / t_b, "batched_ms_per_launch": 1e3 * t_b,
             "per_molecule_fock_builds_per_s": rate_single,
@@ -304,7 +313,10 @@ def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3):
             "tuning": {"streams": tun.streams, "grids": tun.grids},
             "scf_time_s": t_scf, "scf_fock_launches": int(br.fock_builds),
             "converged": int(br.converged.sum()), "setup_s": t_setup,
-            "mean_energy": float(np.mean(E))}
+            "mean_energy": float(np.mean(E)),
+            "parity_vs_single_molecule": {"molecules": int(len(pick)), "max_abs_energy_diff_Eh": float(max(dE)),
+                                          "sample": "seeded random subset (numpy default_rng(4242))",
+                                          "energies": "FP64 polish build of each converged density, both paths"}}
 
 
 def mixed_bench(n_water=32, thr=1e-5, conver=1e-8, seed=32):
@@ -385,14 +397,26 @@ METRIC = ("RHF time-to-converge (1e-8 Eh) & Fock builds/s on 1 GB300: chosen for
 TTC_RUNS = 2
 
 
+def reference_energies_h2o8():
+    """{seed: energy} of the reference's conventional RHF (conver 1e-12) on held-out
+    (H2O)8 / 6-31G clusters (tests/golden/h2o8_631g_reference.json, made by
+    tests/golden/make_golden_h2o8.py from the reference itself)."""
+    path = os.path.join(REPO, "tests", "golden", "h2o8_631g_reference.json")
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return {int(m["seed"]): float(m["energy"]) for m in json.load(f)["molecules"]}
+
+
 def combined_bench(nmol=64, thr=COMBINED_FP32_BELOW, conver=1e-8):
     """The three changes together on held-out seeded (H2O)8 clusters (6-31G): the plain
     FP64 GPU path (one Molecule(...).RHF(direct=True) after another, core guess) vs
     one BatchRHF over all molecules with FP32 below Schwarz thr and the learned guess
     (energies from an FP64 polish build), with two ablations (batched FP64 core
     guess, batched mixed core guess).  Times are wall clock from geometry strings to
-    converged energies (set-up included).  Energy errors are against the FP64
-    oracle energy of each molecule: the polished energy of the plain path's density."""
+    converged energies (set-up included).  Energy errors are against the reference's
+    own conventional RHF energies (conver 1e-12) of the first eight molecules; the
+    differences to the plain FP64 GPU path's polished energies cover all of them."""
     import numpy as np
     import torch
     from mmd import guess as G
@@ -412,11 +436,21 @@ def combined_bench(nmol=64, thr=COMBINED_FP32_BELOW, conver=1e-8):
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t0
     Ep = np.array(Ep)
-    Eo = np.array([_polished_energy(m) for m in mols])
+    Eo = np.array([_polished_energy(m) for m in mols])  # plain FP64 GPU path, polished
+    ref = reference_energies_h2o8()  # the reference's own conventional RHF, conver 1e-12
+    ridx = [k for k in range(nmol) if 900000 + k in ref]
+    Er = np.array([ref[900000 + k] for k in ridx])
+
+    def vs_ref(E):
+        return float(np.abs(np.asarray(E)[ridx] - Er).max()) if ridx else None
+
     out = {"molecules": nmol, "workload": "(H2O)8 6-31G, seeds 900000+k (held out from training)",
            "conver": conver, "fp32_below": thr,
+           "reference_energies": {"molecules": len(ridx), "source": "tests/golden/h2o8_631g_reference.json: the "
+                                  "reference's conventional RHF (its compiled Cython doERIs), conver 1e-12"},
            "plain_fp64": {"time_to_converge_s": t_plain, "mean_iterations": float(np.mean(itp)),
-                          "max_abs_energy_error_vs_oracle": float(np.abs(Ep - Eo).max())}}
+                          "max_abs_energy_error_vs_reference": vs_ref(Ep),
+                          "max_abs_energy_error_polished_vs_reference": vs_ref(Eo)}}
     net = G.DensityMLP.load()
     for name, fp, learned in (("batched_fp64_core", 0.0, False), ("batched_mixed_core", thr, False),
                               ("batched_mixed_learned", thr, True)):
@@ -429,8 +463,9 @@ def combined_bench(nmol=64, thr=COMBINED_FP32_BELOW, conver=1e-8):
         t = time.perf_counter() - t0
         out[name] = {"time_to_converge_s": t, "speedup_vs_plain": t_plain / t,
                      "mean_iterations": float(br.iterations.mean()), "converged": int(br.converged.sum()),
-                     "max_abs_energy_error_vs_oracle": float(np.abs(E - Eo).max()),
-                     "max_abs_energy_error_vs_oracle_unpolished": float(np.abs(br.energies_raw - Eo).max())}
+                     "max_abs_energy_error_vs_reference": vs_ref(E),
+                     "max_abs_energy_diff_vs_plain_fp64_gpu_all": float(np.abs(E - Eo).max()),
+                     "max_abs_energy_error_vs_reference_unpolished": vs_ref(br.energies_raw)}
         if learned:
             out[name]["reverted_to_core"] = int(br.reverted.sum())
     return out
@@ -483,7 +518,8 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=COMBINED_FP32_B
     """Time to converge of the benchmark molecule in the chosen form -- learned initial
     guess (6-31G network, embedded in 6-31G**), FP32 below Schwarz thr, FP64 polish --
     against the plain FP64 path's time (measured just before, fresh context) and the
-    FP64 oracle energy (polished energy of the plain path's converged density)."""
+    plain FP64 GPU path's polished energy (the reference's own SCF at N = 400 would take
+    days; the plain path is pinned to the reference at the smaller sizes)."""
     import torch
     from mmd import guess as G
     from mmd.integrals import twoe
@@ -503,8 +539,8 @@ def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=COMBINED_FP32_B
             "iterations": int(m.iterations), "guess_reverted": bool(m.guess_reverted),
             "iterations_s": float(m.scf_time), "plain_iterations_s": float(plain_mol.scf_time),
             "speedup_vs_plain_fp64": ttc_plain / t, "plain_fp64_iterations": iters_plain,
-            "energy": E, "energy_error_vs_fp64_oracle": E - E_oracle,
-            "plain_fp64_energy_error_vs_oracle": float(plain_mol.energy) - E_oracle}
+            "energy": E, "energy_diff_vs_plain_fp64_gpu_polished": E - E_oracle,
+            "plain_fp64_energy_diff_vs_its_polished": float(plain_mol.energy) - E_oracle}
 
 
 def fp64_roofline(class_ms, counts, builds, fp64_peak):
