@@ -660,6 +660,8 @@ def gpu_arm(args):
     fp64_peak, fp32_peak = _native.measure_peaks(ctx)
     roofline = fp64_roofline(class_ms, counts, builds, fp64_peak)
     roofline["fp32_peak"] = fp32_peak
+    # the FP64 tensor cores beside the DFMA pipe (why the transforms stay on DFMA)
+    roofline["fp64_pipes"] = _native.measure_fp64_pipes(ctx, 16)
     if WORKLOAD["n_water"] == 16:
         key = roofline["class"]
         roofline["traffic"] = DRAM_BYTES_PER_LAUNCH.get(key)

@@ -153,6 +153,14 @@ int mmdg_fock_timed(mmdg_context* ctx, const double* dP, double* G, double tol, 
  * Measurement support; no counterpart in the reference. */
 int mmdg_measure_peaks(mmdg_context* ctx, double* fp64_tflops, double* fp32_tflops);
 
+/* The FP64 pipes of this GPU, with `warps_per_sm` warps per SM: res[0] = DFMA
+ * TFLOP/s (8 independent FMA chains per thread), res[1] = FP64 tensor-core TFLOP/s
+ * (8 independent mma.sync m8n8k4 f64 chains per warp), res[2..4] = the device times
+ * (ms) of the DFMA kernel, the tensor-core kernel and one kernel issuing both
+ * streams: res[4] near max(res[2], res[3]) means the two overlap, near the sum that
+ * they share one resource.  Measurement support; no counterpart in the reference. */
+int mmdg_measure_fp64_pipes(mmdg_context* ctx, int warps_per_sm, double* res);
+
 /* Host copy of the Boys interpolation table (no GPU needed): rows (L, k) of
  * F_{L+n}(k/16)/n! (n = 0..6, 8 doubles per row, L = 0..8, k = 0..767) followed by
  * rows k of exp(-k/16)/n! (n = 0..7).  With out = NULL returns the length; else

@@ -1611,6 +1611,88 @@ extern "C" int mmdg_measure_peaks(mmdg_context* h, double* fp64_tflops, double* 
   return MMDG_OK;
 }
 
+// FP64 pipes of this GPU: independent DFMA chains, independent FP64 tensor-core
+// chains (mma.sync m8n8k4 f64: 512 FLOPs per warp instruction), and both in one
+// kernel -- whether the two run side by side (time of both ~ the longer alone) or
+// share one resource (time of both ~ the sum).  This is the measurement behind
+// the choice of CUDA-core FP64 for the ERI transforms.
+__device__ __forceinline__ void dmma_m8n8k4(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+
+template <bool FMA, bool MMA>
+__global__ void k_fp64_pipe_probe(double* out, int iters_fma, int iters_mma, double a, double b) {
+  double x[8], c0[8], c1[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    x[k] = threadIdx.x + k;
+    c0[k] = 1e-3 * k;
+    c1[k] = 2e-3 * k;
+  }
+  const int iters = FMA && MMA ? (iters_fma > iters_mma ? iters_fma : iters_mma) : (FMA ? iters_fma : iters_mma);
+  for (int i = 0; i < iters; ++i) {
+    if (FMA && i < iters_fma) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+    }
+    if (MMA && i < iters_mma) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) dmma_m8n8k4(c0[k], c1[k], a, b);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k] + c0[k] + c1[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+extern "C" int mmdg_measure_fp64_pipes(mmdg_context* h, int warps_per_sm, double* res) {
+  if (!h || !res) return fail(MMDG_E_ARG, "mmdg_measure_fp64_pipes: null argument");
+  if (warps_per_sm < 1 || warps_per_sm > 64) return fail(MMDG_E_ARG, "mmdg_measure_fp64_pipes: 1..64 warps per SM");
+  DeviceGuard dg(h->device);
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  const int threads = 256, blocks = sms * ((warps_per_sm * 32 + threads - 1) / threads);
+  DevBuf<double> out;
+  if (out.alloc((size_t)blocks * threads)) return fail(MMDG_E_NOMEM, "mmdg_measure_fp64_pipes: allocation");
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  const int it_fma = 200, it_mma = 400;
+  float ms[3] = {0.f, 0.f, 0.f};
+  for (int rep = 0; rep < 2; ++rep) {  // first pass warms up
+    CUDA_TRY(cudaEventRecord(e0));
+    k_fp64_pipe_probe<true, false><<<blocks, threads>>>(out.p, it_fma, it_mma, 0.999, 1e-3);
+    CUDA_TRY(cudaEventRecord(e1));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    CUDA_TRY(cudaEventElapsedTime(&ms[0], e0, e1));
+    CUDA_TRY(cudaEventRecord(e0));
+    k_fp64_pipe_probe<false, true><<<blocks, threads>>>(out.p, it_fma, it_mma, 0.999, 1e-3);
+    CUDA_TRY(cudaEventRecord(e1));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    CUDA_TRY(cudaEventElapsedTime(&ms[1], e0, e1));
+    CUDA_TRY(cudaEventRecord(e0));
+    k_fp64_pipe_probe<true, true><<<blocks, threads>>>(out.p, it_fma, it_mma, 0.999, 1e-3);
+    CUDA_TRY(cudaEventRecord(e1));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    CUDA_TRY(cudaEventElapsedTime(&ms[2], e0, e1));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CUDA_TRY(cudaGetLastError());
+  const double nthr = double(blocks) * threads;
+  res[0] = 2.0 * 64 * it_fma * nthr / (ms[0] * 1e-3) / 1e12;                 // DFMA TFLOP/s
+  res[1] = 512.0 * 8 * it_mma * (nthr / 32) / (ms[1] * 1e-3) / 1e12;        // DMMA TFLOP/s
+  res[2] = ms[0];
+  res[3] = ms[1];
+  res[4] = ms[2];
+  return MMDG_OK;
+}
+
 void mmdg_fill_boys_table(double* t64) { build_boys_table_raw(t64, nullptr); }
 
 // host copy of the Boys interpolation table (no GPU needed): for tests

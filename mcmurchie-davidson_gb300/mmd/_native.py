@@ -55,6 +55,7 @@ def _bind(L):
         "mmdg_device_bytes": (c_int, [p, ctypes.POINTER(c_ll)]),
         "mmdg_ao2mo": (c_int, [c_ll, p, p, p, p, p]),
         "mmdg_rsqrt": (c_int, [p, c_ll, p, p, p, p]),
+        "mmdg_measure_fp64_pipes": (c_int, [p, c_int, p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -280,6 +281,16 @@ def measure_peaks(ctx) -> tuple[float, float]:
     b = ctypes.c_double()
     check(lib().mmdg_measure_peaks(ctx._h, ctypes.byref(a), ctypes.byref(b)), "mmdg_measure_peaks")
     return a.value, b.value
+
+
+def measure_fp64_pipes(ctx, warps_per_sm: int = 16) -> dict:
+    """DFMA and FP64 tensor-core (DMMA) throughput and whether they overlap
+    (mmdg_measure_fp64_pipes)."""
+    r = np.zeros(5)
+    check(lib().mmdg_measure_fp64_pipes(ctx._h, int(warps_per_sm), _ptr(r)), "mmdg_measure_fp64_pipes")
+    return {"warps_per_sm": int(warps_per_sm), "dfma_tflops": float(r[0]), "dmma_tflops": float(r[1]),
+            "dfma_ms": float(r[2]), "dmma_ms": float(r[3]), "both_ms": float(r[4]),
+            "both_over_sum": float(r[4] / (r[2] + r[3])), "both_over_max": float(r[4] / max(r[2], r[3]))}
 
 
 _default_ctx = None

@@ -212,13 +212,31 @@ class Molecule(SCF, Forces):
     def build(self, direct=False):
         """One-electron integrals, then the Schwarz table (direct) or the ERI tensor (molecule.py:90-102)."""
         self.one_electron_integrals()
-        if direct:
-            scr = self.context.screen()
-            self.screen = {pq: float(v) for pq, v in enumerate(scr)}
-            self._screen_array = scr
-        else:
+        # the Schwarz table stays on the device (the SCF's Fock builds screen there);
+        # ``screen`` fetches it and builds the reference's dict on first access
+        self.__dict__.pop("_screen_dict", None)
+        self.__dict__.pop("_screen_array", None)
+        if not direct:
             self.two_electron_integrals()
         self.is_built = True
+
+    @property
+    def screen(self):
+        """The Schwarz dict screen[p(p+1)/2 + q] = (pq|pq) of Molecule.build
+        (mmd/molecule.py:95-99), built from the device table on first access."""
+        d = self.__dict__.get("_screen_dict")
+        if d is None:
+            arr = self.__dict__.get("_screen_array")
+            if arr is None:
+                arr = self.context.screen()
+                self._screen_array = arr
+            d = {pq: float(v) for pq, v in enumerate(arr)}
+            self._screen_dict = d
+        return d
+
+    @screen.setter
+    def screen(self, value):
+        self._screen_dict = value
 
     def one_electron_integrals(self):
         """S, T, V, dipole integrals on the GPU; Core = T + V; X = S^-1/2, U = S^1/2 (molecule.py:235-286)."""

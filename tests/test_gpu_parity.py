@@ -314,3 +314,12 @@ def test_primitive_pair_screening_is_below_the_parity_tolerance():
     T0 = _native.Context(ws, prim_tol=0.0).eri_tensor().cpu().numpy()
     T1 = _native.Context(ws).eri_tensor().cpu().numpy()
     assert np.abs(T1 - T0).max() < 1e-14
+
+
+def test_fp64_pipe_probe_reports_both_pipes():
+    """mmdg_measure_fp64_pipes: DFMA and FP64 tensor-core rates are positive and the
+    combined kernel takes at least as long as either stream alone."""
+    from mmd import _native
+    r = _native.measure_fp64_pipes(_native.scratch_context(), 8)
+    assert r["dfma_tflops"] > 0.1 and r["dmma_tflops"] > 0.1
+    assert r["both_ms"] >= 0.9 * max(r["dfma_ms"], r["dmma_ms"])

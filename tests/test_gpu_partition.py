@@ -56,7 +56,9 @@ def test_partition_parts_match_oracle_parts_and_add_up(name, world):
     finally:
         ctx.set_partition(0, 1)
     assert np.abs(total - full).max() < 1e-12
-    assert np.abs(ctx.fock(dP, tol=1e-12).cpu().numpy() - full).max() == 0.0  # sharding off again
+    # sharding off again: the full build (G accumulates by FP64 atomics, so repeated
+    # builds agree to rounding, not bit for bit)
+    assert np.abs(ctx.fock(dP, tol=1e-12).cpu().numpy() - full).max() < 1e-13
 
 
 def test_sharded_fock_builds_a_direct_rhf_on_one_rank_group():

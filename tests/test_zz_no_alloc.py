@@ -74,10 +74,13 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(built_lib):
     assert b"64 shells" in lib.mmdg_last_error()
     # non-finite inputs are rejected like mmdg_set_basis does, before any GPU work
     m = 2
+    # every array is held in a name for the duration of the call (a temporary would be
+    # freed before the library reads it)
     func = np.array([[i, -1, -1, -1, -1, -1] for i in range(m)], dtype=np.int32)
+    Lm, Km, co = np.zeros(m, dtype=np.int32), np.ones(m, dtype=np.int32), np.ones(m)
     for exps, cen, word in ((np.array([1.0, np.inf]), np.zeros((m, 3)), b"finite"),
                             (np.ones(m), np.array([[0.0, 0.0, 0.0], [np.nan, 0.0, 0.0]]), b"centre")):
-        rc = lib.mmdg_eri_tensor_noalloc(m, p(np.zeros(m, dtype=np.int32)), p(np.ones(m, dtype=np.int32)), p(cen),
-                                         p(exps), p(np.ones(m)), p(func), m, ctypes.c_void_p(out.data_ptr()), None)
+        rc = lib.mmdg_eri_tensor_noalloc(m, p(Lm), p(Km), p(cen), p(exps), p(co), p(func), m,
+                                         ctypes.c_void_p(out.data_ptr()), None)
         assert rc != 0
         assert word in lib.mmdg_last_error()
