@@ -33,6 +33,7 @@
 namespace mmdg {
 
 constexpr int kWarps = kThreads / 32;
+constexpr int kItem = 8;  // list quartets per warp work item (k_fock_warp)
 
 __device__ __forceinline__ int herm_index(int t, int u, int v) {
   const int n = t + u + v, m = n - t;
@@ -90,150 +91,205 @@ __global__ void __launch_bounds__(kThreads) k_fock_warp(Geometry g, FockArgs f, 
   Real* const Bq = R1 + HL;
   Real* const Rfin = (L & 1) ? R1 : R0;  // level L lands in buffer L % 2
   const unsigned n = s_pre[nkeys];
-  unsigned nfq = 0, nsq = 0, npq = 0, nbp = 0, nas = 0, c_nasym_total = 0;
-  int key = 0;
-  for (unsigned qi = blockIdx.x * kWarps + warp; qi < n; qi += gridDim.x * kWarps) {
-    if (qi < s_pre[key]) key = 0;
-    while (qi >= s_pre[key + 1]) ++key;
-    const int2 e = list[s_off[key] + (qi - s_pre[key])];
-    const int bp = __ldg(cl.bra + e.x), kp = __ldg(cl.ket + e.y);
-    const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
-    Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, nullptr);
-    c.nasym = 0;
-    const int nbra = c.bra_end - c.bra_begin, nket = c.ket_end - c.ket_begin, nprim = nbra * nket;
-    Real acc[NBO];
+  constexpr unsigned kFull = 0xffffffffu;
+  unsigned nfq = 0, nsq = 0, npq = 0, nbp = 0, nas = 0;
+  // Work item: kItem consecutive list quartets (one bucket, mostly: equal primitive
+  // counts).  Their primitive quartets are grouped into batches of at most 32, whose
+  // Boys functions the lanes evaluate together; a quartet with more than 32 primitive
+  // quartets is evaluated alone, 32 at a time.
+  for (unsigned q0 = (blockIdx.x * kWarps + warp) * kItem; q0 < n; q0 += gridDim.x * kWarps * kItem) {
+    const int nq = (int)min((unsigned)kItem, n - q0);
+    int qbp = 0, qkp = 0, qnp = 0;  // lane x < nq: quartet x of the item
+    if (lane < nq) {
+      const unsigned qi = q0 + lane;
+      int key = 0;
+      while (qi >= s_pre[key + 1]) ++key;
+      const int2 e = list[s_off[key] + (qi - s_pre[key])];
+      qbp = __ldg(cl.bra + e.x);
+      qkp = __ldg(cl.ket + e.y);
+      qnp = __ldg(g.pr_count + qbp) * __ldg(g.pr_count + qkp);
+    }
+    int qend = qnp;  // inclusive prefix sum of the primitive-quartet counts
 #pragma unroll
-    for (int m = 0; m < NBO; ++m) acc[m] = Real(0);
-    for (int o = lane; o < NCD * HP; o += 32) Ws[o] = Real(0);
-    for (int i = 0; i < nbra; ++i) {
-      for (int j = 0; j < nket; ++j) {
-        const int p = i * nket + j;
-        if ((p & 31) == 0) {  // Boys and R^(n)_000 of the next 32 primitive quartets
-          __syncwarp();
-          const int pp = p + lane;
-          if (pp < nprim) {
-            const int ii = pp / nket, jj = pp - ii * nket;
-            Real Rn[L + 1], X, Y, Z;
-            c.template hermite_r0_pp<L>(c.pp(c.bra_begin + ii), c.pp(c.ket_begin + jj), Rn, X, Y, Z);
-            Real* b = Bq + lane * SM::BQ;
-#pragma unroll
-            for (int k = 0; k <= L; ++k) b[k] = Rn[k];
-            b[L + 1] = X;
-            b[L + 2] = Y;
-            b[L + 3] = Z;
-          }
-          __syncwarp();
-        }
-        // ---- Hermite Coulomb recursion, level by level
-        const Real* b = Bq + (p & 31) * SM::BQ;
-        const Real X = b[L + 1], Y = b[L + 2], Z = b[L + 3];
-        if (lane == 0) R0[0] = b[L];
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(kFull, qend, d);
+      if (lane >= d) qend += t;
+    }
+    int qs = 0;
+    while (qs < nq) {
+      const int prev = __shfl_sync(kFull, qend, qs > 0 ? qs - 1 : 0);
+      const int base = qs > 0 ? prev : 0;
+      const bool fits = lane >= qs && lane < nq && qend - base <= 32;
+      int qe = qs + __popc(__ballot_sync(kFull, fits));
+      const bool batched = qe > qs;
+      if (!batched) qe = qs + 1;
+      if (batched) {  // Boys and R^(n)_000 of every primitive quartet of quartets qs..qe-1
         __syncwarp();
+        const int tot = __shfl_sync(kFull, qend, qe - 1) - base;
+        int myq = qs;
+        for (int x = qs; x < qe - 1; ++x)
+          if (lane >= __shfl_sync(kFull, qend, x) - base) myq = x + 1;
+        const int mbp = __shfl_sync(kFull, qbp, myq), mkp = __shfl_sync(kFull, qkp, myq);
+        const int mprev = __shfl_sync(kFull, qend, myq > 0 ? myq - 1 : 0);  // every lane shuffles
+        const int mstart = (myq > qs ? mprev : base) - base;
+        if (lane < tot) {
+          Ctx<Real> cq = make_ctx<MD, Real>(g, mbp, mkp, nullptr);
+          const int nk = cq.ket_end - cq.ket_begin;
+          const int pp = lane - mstart, ii = pp / nk, jj = pp - ii * nk;
+          Real Rn[L + 1], X, Y, Z;
+          cq.template hermite_r0_pp<L>(cq.pp(cq.bra_begin + ii), cq.pp(cq.ket_begin + jj), Rn, X, Y, Z);
+          Real* b = Bq + lane * SM::BQ;
 #pragma unroll
-        for (int s = 1; s <= L; ++s) {
-          const Real* src = (s & 1) ? R0 : R1;
-          Real* dst = (s & 1) ? R1 : R0;
-          const int hs = (s + 1) * (s + 2) * (s + 3) / 6;
-          for (int x = lane; x < hs; x += 32) {
-            const int tuv = s_herm[x];
-            const int t = tuv & 31, u = (tuv >> 5) & 31, v = tuv >> 10;
-            // the first non-zero index steps down: (t-1) with X, else (u-1) with Y, else (v-1) with Z
-            const int d = t > 0 ? 0 : (u > 0 ? 1 : 2);
-            const int m1 = d == 0 ? t : (d == 1 ? u : v);
-            const Real C = d == 0 ? X : (d == 1 ? Y : Z);
-            const int i1 = herm_index(t - (d == 0), u - (d == 1), v - (d == 2));
-            const int i2 = m1 > 1 ? herm_index(t - 2 * (d == 0), u - 2 * (d == 1), v - 2 * (d == 2)) : 0;
-            Real val = C * src[x == 0 ? 0 : i1];
-            val = fma(Real(m1 > 1 ? m1 - 1 : 0), src[i2], val);
-            dst[x] = x == 0 ? b[L - s] : val;
-          }
-          __syncwarp();
+          for (int k = 0; k <= L; ++k) b[k] = Rn[k];
+          b[L + 1] = X;
+          b[L + 2] = Y;
+          b[L + 3] = Z;
+          nas += cq.nasym;
         }
-        // ---- ket transform into W[cd][h]
-        const Real* __restrict__ ek = c.ket_E(c.ket_begin + j);
-        for (int m = 0; m < NKO; ++m) {
-          const int o = m * 32 + lane;
-          const bool act = o < NCD * HP;
-          const int cd = act ? o / HP : 0, h = act ? o - cd * HP : 0;
-          const unsigned rec = s_ket[cd];
-          const int nt = fp_nt(rec), nu = fp_nu(rec), np = fp_np(rec);
-          const int cnt = act ? nt * nu * np : 0;
-          const int maxc = __reduce_max_sync(0xffffffffu, cnt);
-          const int ht = s_herm[h];
-          const int th = ht & 31, uh = (ht >> 5) & 31, vh = ht >> 10;
-          const Real* __restrict__ ep = ek + fp_eoff(rec);
-          Real w = act ? Ws[o] : Real(0);
-          int ta = 0, nv = 0, ph = 0;
-          for (int k = 0; k < maxc; ++k) {
-            const bool in = k < cnt;
-            const Real ev = in ? ep[k] : Real(0);
-            const Real r = Rfin[in ? herm_index(th + ta, uh + nv, vh + ph) : 0];
-            w = fma(((ta + nv + ph) & 1) ? -ev : ev, r, w);
-            if (++ph == np) {
-              ph = 0;
-              if (++nv == nu) {
-                nv = 0;
-                ++ta;
+        __syncwarp();
+      }
+      for (int x = qs; x < qe; ++x) {
+        const int bp = __shfl_sync(kFull, qbp, x), kp = __shfl_sync(kFull, qkp, x);
+        const int xprev = __shfl_sync(kFull, qend, x > 0 ? x - 1 : 0);
+        const int boff = batched ? (x > qs ? xprev : base) - base : 0;  // Bq slot of its first primitive quartet
+        const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
+        Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, nullptr);
+        const int nbra = c.bra_end - c.bra_begin, nket = c.ket_end - c.ket_begin, nprim = nbra * nket;
+        Real acc[NBO];
+#pragma unroll
+        for (int m = 0; m < NBO; ++m) acc[m] = Real(0);
+        for (int o = lane; o < NCD * HP; o += 32) Ws[o] = Real(0);
+        for (int i = 0; i < nbra; ++i) {
+          for (int j = 0; j < nket; ++j) {
+            const int p = i * nket + j;
+            if (!batched && (p & 31) == 0) {  // a large quartet: 32 primitive quartets at a time
+              __syncwarp();
+              const int pp = p + lane;
+              if (pp < nprim) {
+                const int ii = pp / nket, jj = pp - ii * nket;
+                Real Rn[L + 1], X, Y, Z;
+                c.template hermite_r0_pp<L>(c.pp(c.bra_begin + ii), c.pp(c.ket_begin + jj), Rn, X, Y, Z);
+                Real* b = Bq + lane * SM::BQ;
+#pragma unroll
+                for (int k = 0; k <= L; ++k) b[k] = Rn[k];
+                b[L + 1] = X;
+                b[L + 2] = Y;
+                b[L + 3] = Z;
+              }
+              __syncwarp();
+            }
+            // ---- Hermite Coulomb recursion, level by level
+            const Real* b = Bq + (batched ? boff + p : (p & 31)) * SM::BQ;
+            const Real X = b[L + 1], Y = b[L + 2], Z = b[L + 3];
+            if (lane == 0) R0[0] = b[L];
+            __syncwarp();
+#pragma unroll
+            for (int s = 1; s <= L; ++s) {
+              const Real* src = (s & 1) ? R0 : R1;
+              Real* dst = (s & 1) ? R1 : R0;
+              const int hs = (s + 1) * (s + 2) * (s + 3) / 6;
+              for (int x2 = lane; x2 < hs; x2 += 32) {
+                const int tuv = s_herm[x2];
+                const int t = tuv & 31, u = (tuv >> 5) & 31, v = tuv >> 10;
+                // the first non-zero index steps down: (t-1) with X, else (u-1) with Y, else (v-1) with Z
+                const int d = t > 0 ? 0 : (u > 0 ? 1 : 2);
+                const int m1 = d == 0 ? t : (d == 1 ? u : v);
+                const Real C = d == 0 ? X : (d == 1 ? Y : Z);
+                const int i1 = herm_index(t - (d == 0), u - (d == 1), v - (d == 2));
+                const int i2 = m1 > 1 ? herm_index(t - 2 * (d == 0), u - 2 * (d == 1), v - 2 * (d == 2)) : 0;
+                Real val = C * src[x2 == 0 ? 0 : i1];
+                val = fma(Real(m1 > 1 ? m1 - 1 : 0), src[i2], val);
+                dst[x2] = x2 == 0 ? b[L - s] : val;
+              }
+              __syncwarp();
+            }
+            // ---- ket transform into W[cd][h]
+            const Real* __restrict__ ek = c.ket_E(c.ket_begin + j);
+            for (int m = 0; m < NKO; ++m) {
+              const int o = m * 32 + lane;
+              const bool act = o < NCD * HP;
+              const int cd = act ? o / HP : 0, h = act ? o - cd * HP : 0;
+              const unsigned rec = s_ket[cd];
+              const int nt = fp_nt(rec), nu = fp_nu(rec), np = fp_np(rec);
+              const int cnt = act ? nt * nu * np : 0;
+              const int maxc = __reduce_max_sync(kFull, cnt);
+              const int ht = s_herm[h];
+              const int th = ht & 31, uh = (ht >> 5) & 31, vh = ht >> 10;
+              const Real* __restrict__ ep = ek + fp_eoff(rec);
+              Real w = act ? Ws[o] : Real(0);
+              int ta = 0, nv = 0, ph = 0;
+              for (int k = 0; k < maxc; ++k) {
+                const bool in = k < cnt;
+                const Real ev = in ? ep[k] : Real(0);
+                const Real r = Rfin[in ? herm_index(th + ta, uh + nv, vh + ph) : 0];
+                w = fma(((ta + nv + ph) & 1) ? -ev : ev, r, w);
+                if (++ph == np) {
+                  ph = 0;
+                  if (++nv == nu) {
+                    nv = 0;
+                    ++ta;
+                  }
+                }
+              }
+              if (act) Ws[o] = w;
+            }
+            __syncwarp();
+          }
+          // ---- bra transform of this bra primitive: acc[ab][cd] += E'_ab . W[cd]
+          const Real* __restrict__ eb = c.bra_E(c.bra_begin + i);
+#pragma unroll
+          for (int m = 0; m < NBO; ++m) {
+            const int o = m * 32 + lane;
+            const bool act = o < NAB * NCD;
+            const int ab = act ? o / NCD : 0, cd = act ? o - ab * NCD : 0;
+            const unsigned rec = s_bra[ab];
+            const int nt = fp_nt(rec), nu = fp_nu(rec), np = fp_np(rec);
+            const int cnt = act ? nt * nu * np : 0;
+            const int maxc = __reduce_max_sync(kFull, cnt);
+            const Real* __restrict__ ep = eb + fp_eoff(rec);
+            const Real* __restrict__ wr = Ws + cd * HP;
+            Real a = acc[m];
+            int ta = 0, nv = 0, ph = 0;
+            for (int k = 0; k < maxc; ++k) {
+              const bool in = k < cnt;
+              const Real ev = in ? ep[k] : Real(0);
+              a = fma(ev, wr[in ? herm_index(ta, nv, ph) : 0], a);
+              if (++ph == np) {
+                ph = 0;
+                if (++nv == nu) {
+                  nv = 0;
+                  ++ta;
+                }
               }
             }
+            acc[m] = a;
           }
-          if (act) Ws[o] = w;
+          __syncwarp();
+          for (int o = lane; o < NCD * HP; o += 32) Ws[o] = Real(0);
+          __syncwarp();
         }
-        __syncwarp();
-      }
-      // ---- bra transform of this bra primitive: acc[ab][cd] += E'_ab . W[cd]
-      const Real* __restrict__ eb = c.bra_E(c.bra_begin + i);
+        if (!batched) nas += c.nasym;
+        // ---- digestion: every lane its function quartets
+        QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, __ldg(g.sh_mol + sa)};
+        FockDigest<NB, ND> dg(g, f, q);
 #pragma unroll
-      for (int m = 0; m < NBO; ++m) {
-        const int o = m * 32 + lane;
-        const bool act = o < NAB * NCD;
-        const int ab = act ? o / NCD : 0, cd = act ? o - ab * NCD : 0;
-        const unsigned rec = s_bra[ab];
-        const int nt = fp_nt(rec), nu = fp_nu(rec), np = fp_np(rec);
-        const int cnt = act ? nt * nu * np : 0;
-        const int maxc = __reduce_max_sync(0xffffffffu, cnt);
-        const Real* __restrict__ ep = eb + fp_eoff(rec);
-        const Real* __restrict__ wr = Ws + cd * HP;
-        Real a = acc[m];
-        int ta = 0, nv = 0, ph = 0;
-        for (int k = 0; k < maxc; ++k) {
-          const bool in = k < cnt;
-          const Real ev = in ? ep[k] : Real(0);
-          a = fma(ev, wr[in ? herm_index(ta, nv, ph) : 0], a);
-          if (++ph == np) {
-            ph = 0;
-            if (++nv == nu) {
-              nv = 0;
-              ++ta;
-            }
+        for (int m = 0; m < NBO; ++m) {
+          const int o = m * 32 + lane;
+          if (o < NAB * NCD) {
+            const int ab = fp_index(s_bra[o / NCD]), cd = fp_index(s_ket[o % NCD]);
+            dg.put(ab / NB, ab % NB, cd / ND, cd % ND, acc[m]);
           }
         }
-        acc[m] = a;
+        nfq += dg.nfq;
+        if (lane == 0) {
+          ++nsq;
+          npq += unsigned(nprim);
+          nbp += unsigned(nbra);
+        }
       }
-      __syncwarp();
-      for (int o = lane; o < NCD * HP; o += 32) Ws[o] = Real(0);
-      __syncwarp();
-    }
-    c_nasym_total += c.nasym;
-    // ---- digestion: every lane its function quartets
-    QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, __ldg(g.sh_mol + sa)};
-    FockDigest<NB, ND> dg(g, f, q);
-#pragma unroll
-    for (int m = 0; m < NBO; ++m) {
-      const int o = m * 32 + lane;
-      if (o < NAB * NCD) {
-        const int ab = fp_index(s_bra[o / NCD]), cd = fp_index(s_ket[o % NCD]);
-        dg.put(ab / NB, ab % NB, cd / ND, cd % ND, acc[m]);
-      }
-    }
-    nfq += dg.nfq;
-    if (lane == 0) {
-      ++nsq;
-      npq += unsigned(nprim);
-      nbp += unsigned(nbra);
+      qs = qe;
     }
   }
-  nas = c_nasym_total;
   if (f.counters) {
     const unsigned s0 = __reduce_add_sync(0xffffffffu, nfq), s1 = __reduce_add_sync(0xffffffffu, nsq),
                    s2 = __reduce_add_sync(0xffffffffu, npq), s3 = __reduce_add_sync(0xffffffffu, nbp),

@@ -95,9 +95,9 @@ def build_flops(counts, kind: str = "model") -> float:
 # code (csrc/gen_md.py, csrc/md_device.cuh, csrc/md_warp.cuh), lane by lane, with an
 # FMA as 2 FLOPs and a multiply or add as 1 -- the quantity that ncu's
 # smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on counters measure as
-# 2 DFMA + DMUL + DADD.  Not counted: the FP64 instructions inside CUDA's rsqrt and
-# exp (library code, called as such), conversions and compares (the ncu summary
-# gives their share).  Per-class inputs are the Fock build's counters: digested
+# 2 DFMA + DMUL + DADD.  Not counted: the FP64 instructions inside CUDA's exp
+# (library code, called only by the asymptotic Boys branch of L >= 5), conversions
+# and compares (the ncu summary gives their share).  Per-class inputs are the Fock build's counters: digested
 # function quartets, shell quartets, primitive quartets, bra-primitive passes and
 # asymptotic-branch Boys evaluations.
 
@@ -116,19 +116,32 @@ def _gm():
     return _gen_md()
 
 
+RSQRT_FLOPS = 8  # rsqrt_dd: y0^2, two FMAs, one product, one FMA (md_device.cuh)
+
+
 def boys_flops(L: int, asymptotic: bool) -> int:
-    """boys_eval<L> (md_device.cuh): Taylor row + exp row + downward recursion, or
-    the asymptotic start F_0 and upward recursion (T >= 48)."""
+    """boys_eval<L> (md_device.cuh).  Taylor branch: y = T_k - T (1), the F_L row (6
+    FMAs); for L = 1 the F_0 row (6 FMAs); for L > 1 the exp row (7 FMAs), 2T and the
+    downward recursion (an FMA and a product per order).  Asymptotic branch (T >= 48):
+    rsqrt_dd(T), F_0, 1/T and the upward recursion (exp(-T) terms from L = 5)."""
     if not asymptotic:
-        return 17 + (15 + 3 * L if L > 0 else 0)
+        if L == 0:
+            return 13
+        if L == 1:
+            return 25
+        return 13 + 14 + 1 + 3 * L
     if L == 0:
-        return 1
-    return 2 + (1 + 3 * L if L > 4 else 2 * L)
+        return RSQRT_FLOPS + 1
+    return RSQRT_FLOPS + 2 + (1 + 3 * L if L > 4 else 2 * L)
 
 
 def r0_flops(L: int, asymptotic: bool) -> int:
-    """hermite_r0_pp<L>: P - Q, |PQ|^2, p + q, alpha, T, Boys, prefactor powers."""
-    return 3 + 5 + 1 + 3 + 1 + boys_flops(L, asymptotic) + 2 + (2 * L + 1)
+    """hermite_r0_pp<L>: P - Q (3), |PQ|^2 (5), p + q (1), rsqrt_dd(p + q), alpha (3),
+    T (1), Boys, the prefactor powers R^(n) = (-2 alpha)^n F_n / sqrt(p+q) (2 pi^{5/2}
+    sits in the E' coefficients): -2 alpha once for L > 0, one product per order and
+    one per step of the power."""
+    pref = 1 if L == 0 else 1 + (2 * L + 1)
+    return 3 + 5 + 1 + RSQRT_FLOPS + 3 + 1 + boys_flops(L, asymptotic) + pref
 
 
 @lru_cache(maxsize=None)
