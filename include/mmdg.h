@@ -105,9 +105,12 @@ int mmdg_eri_tensor(mmdg_context* ctx, double* out, void* stream);
  *            out[q*1296 + ((ca*6 + cb)*6 + cc)*6 + cd] for the components ca of a, cb of
  *            b, ... in the component order of mmdg_set_basis; entries beyond a shell's
  *            component count are zero
+ *   precision 0: the FP64 class code (the plain method); 1: the FP32 class code that
+ *            mixed-precision Fock builds use for quartets below their threshold (its
+ *            results widened to double), for measuring that path's per-ERI error
  * Synchronises `stream` before returning.
  */
-int mmdg_eri_quartets(mmdg_context* ctx, long long n, const int* shells, double* out, void* stream);
+int mmdg_eri_quartets(mmdg_context* ctx, long long n, const int* shells, double* out, int precision, void* stream);
 
 /*
  * Sharded direct Fock build: the bra-pair loop of formPT (cython/fock.pyx:38-44)

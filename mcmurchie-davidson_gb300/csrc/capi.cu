@@ -893,8 +893,10 @@ extern "C" int mmdg_eri_tensor(mmdg_context* h, double* out, void* stream) {
 // first, the pair of higher class as the bra -- grouped by angular class and
 // evaluated by one thread each; the digest writes every component back in the
 // caller's order.
-extern "C" int mmdg_eri_quartets(mmdg_context* h, long long n, const int* shells, double* out, void* stream) {
+extern "C" int mmdg_eri_quartets(mmdg_context* h, long long n, const int* shells, double* out, int precision,
+                                 void* stream) {
   if (!h || (n > 0 && (!shells || !out))) return fail(MMDG_E_ARG, "mmdg_eri_quartets: null argument");
+  if (precision != 0 && precision != 1) return fail(MMDG_E_ARG, "mmdg_eri_quartets: precision must be 0 or 1");
   if (!h->have_basis) return fail(MMDG_E_STATE, "mmdg_eri_quartets: no basis set");
   if (n < 0 || n > 0x7fffffffLL / kQuartetBlock) return fail(MMDG_E_ARG, "mmdg_eri_quartets: bad quartet count");
   if (n == 0) return MMDG_OK;
@@ -954,7 +956,7 @@ extern "C" int mmdg_eri_quartets(mmdg_context* h, long long n, const int* shells
   int ci = 0;
   for (const ClassEntry& e : kClasses) {
     const int cnt = (int)(beg[ci + 1] - beg[ci]);
-    if (cnt) CUDA_TRY(e.quartets(g, qa, d_items.p + beg[ci], cnt, st));
+    if (cnt) CUDA_TRY(e.quartets(precision, g, qa, d_items.p + beg[ci], cnt, st));
     ++ci;
   }
   CUDA_TRY(cudaStreamSynchronize(st));  // the item list is released on return

@@ -425,7 +425,7 @@ def generate_instances(outdir, ngroups=6):
             "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
-            "typedef cudaError_t (*quartets_fn)(const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);",
+            "typedef cudaError_t (*quartets_fn)(int, const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);",
             "struct ClassEntry { int la, lb, lc, ld; fock_fn fock; tensor_fn tensor; schwarz_fn schwarz; quartets_fn quartets; };"]
     for g in range(ngroups):
         decl.append(f"cudaError_t init_group{g}();")
@@ -433,7 +433,7 @@ def generate_instances(outdir, ngroups=6):
         s = "".join(map(str, c))
         decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);")
         decl.append(f"cudaError_t launch_tensor_{s}(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);")
-        decl.append(f"cudaError_t launch_quartets_{s}(const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);")
+        decl.append(f"cudaError_t launch_quartets_{s}(int, const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);")
         if c[:2] == c[2:]:
             decl.append(f"cudaError_t launch_schwarz_{s}(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);")
     decl.append("static const ClassEntry kClasses[] = {")
@@ -469,11 +469,13 @@ def generate_instances(outdir, ngroups=6):
             t.append(f"  k_tensor<{md}<double>><<<grid, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, cl);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
-            t.append(f"cudaError_t launch_quartets_{s}(const Geometry& g, const QuartetArgs& a, const QuartetItem* items, int n, cudaStream_t st) {{")
-            t.append(f"  k_quartets<{md}<double>><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, items, n);")
+            t.append(f"cudaError_t launch_quartets_{s}(int prec, const Geometry& g, const QuartetArgs& a, const QuartetItem* items, int n, cudaStream_t st) {{")
+            t.append(f"  if (prec) k_quartets<{md}<float>, float><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, a, items, n);")
+            t.append(f"  else k_quartets<{md}<double>, double><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, items, n);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
-            inits.append(f"  if ((e = cudaFuncSetAttribute(k_quartets<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
+            for real in ("double", "float"):
+                inits.append(f"  if ((e = cudaFuncSetAttribute(k_quartets<{md}<{real}>, {real}>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<{real}>, {real}>()))) return e;")
             if is_warp_class(c):
                 for real in ("double", "float"):
                     mw = f"MDW_{s}<{real}>"
@@ -481,6 +483,10 @@ def generate_instances(outdir, ngroups=6):
             else:
                 inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<double>, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
                 inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<float>, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<float>, float>()))) return e;")
+                inits.append("#ifdef MMDG_EXP_CARVEOUT_L1")
+                for real in ("double", "float"):
+                    inits.append(f"  if (!{md}<{real}>::RSMEM && (e = cudaFuncSetAttribute(k_fock<{md}<{real}>, {real}>, cudaFuncAttributePreferredSharedMemoryCarveout, 0))) return e;")
+                inits.append("#endif")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_tensor<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             if c[:2] == c[2:]:
                 t.append(f"cudaError_t launch_schwarz_{s}(const Geometry& g, const SchwarzArgs& a, const int* list, int n, cudaStream_t st) {{")

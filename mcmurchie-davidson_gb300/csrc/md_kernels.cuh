@@ -206,14 +206,14 @@ __global__ void __launch_bounds__(kThreads) k_tensor(Geometry g, TensorArgs t, C
 }
 
 // listed shell quartets of one class (mmdg_eri_quartets): one thread per item
-template <class MD>
+template <class MD, typename Real>
 __global__ void __launch_bounds__(kThreads) k_quartets(Geometry g, QuartetArgs a, const QuartetItem* items, int n) {
   const int idx = blockIdx.x * kThreads + threadIdx.x;
   if (idx >= n) return;
   const QuartetItem it = items[idx];
   extern __shared__ double smem_d[];
-  double* rs = smem_d + threadIdx.x;
-  Ctx<double> c = make_ctx<MD, double>(g, it.bra, it.ket, rs);
+  Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
+  Ctx<Real> c = make_ctx<MD, Real>(g, it.bra, it.ket, rs);
   QuartetDigest<ncart(MD::LB), ncart(MD::LD)> dg(a, it.slot, it.flags);
   MD::run(c, dg);
 }

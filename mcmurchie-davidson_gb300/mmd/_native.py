@@ -50,7 +50,7 @@ def _bind(L):
         "mmdg_set_prim_tol": (c_int, [p, ctypes.c_double]),
         "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, c_d, p, p]),
         "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),
-        "mmdg_eri_quartets": (c_int, [p, c_ll, p, p, p]),
+        "mmdg_eri_quartets": (c_int, [p, c_ll, p, p, c_int, p]),
         "mmdg_set_partition": (c_int, [p, c_int, c_int, p, c_ll]),
         "mmdg_device_bytes": (c_int, [p, ctypes.POINTER(c_ll)]),
         "mmdg_ao2mo": (c_int, [c_ll, p, p, p, p, p]),
@@ -176,19 +176,20 @@ class Context:
         check(lib().mmdg_eri_tensor(self._h, ctypes.c_void_p(out.data_ptr()), stream_ptr()), "mmdg_eri_tensor")
         return out
 
-    def eri_quartets(self, shells, out=None):
+    def eri_quartets(self, shells, out=None, fp32: bool = False):
         """All component ERIs of listed shell quartets: ``shells`` is an (n, 4) array of
         global shell indices (a, b, c, d); returns a device tensor (n, 6, 6, 6, 6) with
         (ab|cd) for components [ca, cb, cc, cd] in the caller's shell order (entries
-        beyond a shell's components are zero)."""
+        beyond a shell's components are zero).  ``fp32``: the FP32 class code of the
+        mixed-precision path instead of the FP64 one."""
         torch = self.torch
         q = np.ascontiguousarray(shells, dtype=np.int32).reshape(-1, 4)
         n = q.shape[0]
         if out is None:
             out = torch.empty((n, MAX_COMP, MAX_COMP, MAX_COMP, MAX_COMP), dtype=torch.float64,
                               device=f"cuda:{self.device}")
-        check(lib().mmdg_eri_quartets(self._h, n, _ptr(q), ctypes.c_void_p(out.data_ptr()), stream_ptr()),
-              "mmdg_eri_quartets")
+        check(lib().mmdg_eri_quartets(self._h, n, _ptr(q), ctypes.c_void_p(out.data_ptr()), 1 if fp32 else 0,
+                                      stream_ptr()), "mmdg_eri_quartets")
         return out
 
     def function_quartets(self, idx, mol: int = 0):
