@@ -465,13 +465,14 @@ def generate_instances(outdir, ngroups=6):
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_tensor_{s}(const Geometry& g, const TensorArgs& a, const ClassLaunch& cl, cudaStream_t st) {{")
-            t.append(f"  dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads);")
+            t.append(f"  dim3 grid(cl.nbra, (cl.nket + kThreads - 1) / kThreads, {md}<double>::NCHUNK);")
             t.append(f"  k_tensor<{md}<double>><<<grid, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, cl);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_quartets_{s}(int prec, const Geometry& g, const QuartetArgs& a, const QuartetItem* items, int n, cudaStream_t st) {{")
-            t.append(f"  if (prec) k_quartets<{md}<float>, float><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, a, items, n);")
-            t.append(f"  else k_quartets<{md}<double>, double><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, items, n);")
+            t.append(f"  const unsigned nb = (unsigned)(((long long)n * {md}<double>::NCHUNK + kThreads - 1) / kThreads);")
+            t.append(f"  if (prec) k_quartets<{md}<float>, float><<<nb, kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, a, items, n);")
+            t.append(f"  else k_quartets<{md}<double>, double><<<nb, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, items, n);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             for real in ("double", "float"):
@@ -490,7 +491,7 @@ def generate_instances(outdir, ngroups=6):
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_tensor<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             if c[:2] == c[2:]:
                 t.append(f"cudaError_t launch_schwarz_{s}(const Geometry& g, const SchwarzArgs& a, const int* list, int n, cudaStream_t st) {{")
-                t.append(f"  k_schwarz<{md}<double>><<<(n + kThreads - 1) / kThreads, kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, list, n);")
+                t.append(f"  k_schwarz<{md}<double>><<<(unsigned)(((long long)n * {md}<double>::NCHUNK + kThreads - 1) / kThreads), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, a, list, n);")
                 t.append(f"  return cudaGetLastError();")
                 t.append("}")
                 inits.append(f"  if ((e = cudaFuncSetAttribute(k_schwarz<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")

@@ -200,34 +200,41 @@ __global__ void __launch_bounds__(kThreads) k_tensor(Geometry g, TensorArgs t, C
   extern __shared__ double smem_d[];
   double* rs = smem_d + threadIdx.x;
   Ctx<double> c = make_ctx<MD, double>(g, bp, kp, rs);
+  c.chunk = MD::NCHUNK > 1 ? (int)blockIdx.z : -1;  // one ket chunk per grid z-slice
   QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, mol};
   TensorDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, t, q);
   MD::run(c, dg);
 }
 
-// listed shell quartets of one class (mmdg_eri_quartets): one thread per item
+// listed shell quartets of one class (mmdg_eri_quartets): one thread per (item, ket
+// chunk), chunk-major
 template <class MD, typename Real>
 __global__ void __launch_bounds__(kThreads) k_quartets(Geometry g, QuartetArgs a, const QuartetItem* items, int n) {
-  const int idx = blockIdx.x * kThreads + threadIdx.x;
-  if (idx >= n) return;
-  const QuartetItem it = items[idx];
+  const long long idx = blockIdx.x * (long long)kThreads + threadIdx.x;
+  if (idx >= (long long)n * MD::NCHUNK) return;
+  const int chunk = (int)(idx / n);
+  const QuartetItem it = items[idx - (long long)chunk * n];
   extern __shared__ double smem_d[];
   Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
   Ctx<Real> c = make_ctx<MD, Real>(g, it.bra, it.ket, rs);
+  c.chunk = MD::NCHUNK > 1 ? chunk : -1;
   QuartetDigest<ncart(MD::LB), ncart(MD::LD)> dg(a, it.slot, it.flags);
   MD::run(c, dg);
 }
 
 // diagonal quartets (ab|ab) of one pair class: the Schwarz table
+// (one thread per (pair, ket chunk), chunk-major)
 template <class MD>
 __global__ void __launch_bounds__(kThreads) k_schwarz(Geometry g, SchwarzArgs s, const int* list, int n) {
-  const int idx = blockIdx.x * kThreads + threadIdx.x;
-  if (idx >= n) return;
-  const int bp = __ldg(list + idx);
+  const long long idx = blockIdx.x * (long long)kThreads + threadIdx.x;
+  if (idx >= (long long)n * MD::NCHUNK) return;
+  const int chunk = (int)(idx / n);
+  const int bp = __ldg(list + (idx - (long long)chunk * n));
   const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp);
   extern __shared__ double smem_d[];
   double* rs = smem_d + threadIdx.x;
   Ctx<double> c = make_ctx<MD, double>(g, bp, bp, rs);
+  c.chunk = MD::NCHUNK > 1 ? chunk : -1;
   QuartetInfo q{sa, sb, sa, sb, sa == sb, sa == sb, true, __ldg(g.sh_mol + sa)};
   SchwarzDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, s, q, bp);
   MD::run(c, dg);
