@@ -1366,12 +1366,18 @@ __device__ void hermite_r_table(const double* boys, double p, double X, double Y
       for (int v = 0; v <= L - t - u; ++v) R[(t * 5 + u) * 5 + v] = cur[t][u][v];
 }
 
+// grid: x = shell pair, y = nucleus of the pair's molecule (one thread per (pair,
+// nucleus), so the nuclear-attraction sums run in parallel); the y = 0 thread also
+// writes S, T and the dipole integrals; V is accumulated with atomics
 __global__ void k_one_electron(OneEArgs a) {
   const int pr = blockIdx.x * blockDim.x + threadIdx.x;
   if (pr >= a.npair) return;
   const int sa = a.pa[pr], sb = a.pb[pr];
   const int la = a.L[sa], lb = a.L[sb];
   const int m = a.sh_mol[sa];
+  const int atom = a.atom_begin[m] + (int)blockIdx.y;
+  if (atom >= a.atom_end[m]) return;
+  const bool first = blockIdx.y == 0;
   const long long base = a.mol_base[m];
   const int N = a.mol_n[m];
   const double Ax = a.center[3 * sa], Ay = a.center[3 * sa + 1], Az = a.center[3 * sa + 2];
@@ -1419,39 +1425,41 @@ __global__ void k_one_electron(OneEArgs a) {
             }
       }
       const double s3 = pow(PI * ip, 1.5) * cK;
-      // overlap, kinetic, dipole
-      int x = 0;
-      for (int xa = la; xa >= 0; --xa)
-        for (int ya = la - xa; ya >= 0; --ya) {
-          const int za = la - xa - ya;
-          for (int xb = lb; xb >= 0; --xb)
-            for (int yb = lb - xb; yb >= 0; --yb, ++x) {
-              const int zb = lb - xb - yb;
-              const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
-                                 comp_norm(zb);
-              const double Sx = E[0][xa][xb][0], Sy = E[1][ya][yb][0], Sz = E[2][za][zb][0];
-              accS[x] += nab * s3 * Sx * Sy * Sz;
-              const int lbv[3] = {xb, yb, zb};
-              const int lav[3] = {xa, ya, za};
-              double Td[3];
-              for (int d = 0; d < 3; ++d) {
-                const int l2 = lbv[d], l1 = lav[d];
-                double t = (2 * l2 + 1) * eb * E[d][l1][l2][0] - 2.0 * eb * eb * E[d][l1][l2 + 2][0];
-                if (l2 >= 2) t += -0.5 * l2 * (l2 - 1) * E[d][l1][l2 - 2][0];
-                Td[d] = t;
+      // overlap, kinetic, dipole (the first nucleus's thread)
+      if (first) {
+        int x = 0;
+        for (int xa = la; xa >= 0; --xa)
+          for (int ya = la - xa; ya >= 0; --ya) {
+            const int za = la - xa - ya;
+            for (int xb = lb; xb >= 0; --xb)
+              for (int yb = lb - xb; yb >= 0; --yb, ++x) {
+                const int zb = lb - xb - yb;
+                const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
+                                   comp_norm(zb);
+                const double Sx = E[0][xa][xb][0], Sy = E[1][ya][yb][0], Sz = E[2][za][zb][0];
+                accS[x] += nab * s3 * Sx * Sy * Sz;
+                const int lbv[3] = {xb, yb, zb};
+                const int lav[3] = {xa, ya, za};
+                double Td[3];
+                for (int d = 0; d < 3; ++d) {
+                  const int l2 = lbv[d], l1 = lav[d];
+                  double t = (2 * l2 + 1) * eb * E[d][l1][l2][0] - 2.0 * eb * eb * E[d][l1][l2 + 2][0];
+                  if (l2 >= 2) t += -0.5 * l2 * (l2 - 1) * E[d][l1][l2 - 2][0];
+                  Td[d] = t;
+                }
+                accT[x] += nab * s3 * (Td[0] * Sy * Sz + Td[1] * Sx * Sz + Td[2] * Sx * Sy);
+                const double Dx = E[0][xa][xb][1] + (P[0] - O[0]) * Sx;
+                const double Dy = E[1][ya][yb][1] + (P[1] - O[1]) * Sy;
+                const double Dz = E[2][za][zb][1] + (P[2] - O[2]) * Sz;
+                accM[0][x] += nab * s3 * Dx * Sy * Sz;
+                accM[1][x] += nab * s3 * Sx * Dy * Sz;
+                accM[2][x] += nab * s3 * Sx * Sy * Dz;
               }
-              accT[x] += nab * s3 * (Td[0] * Sy * Sz + Td[1] * Sx * Sz + Td[2] * Sx * Sy);
-              const double Dx = E[0][xa][xb][1] + (P[0] - O[0]) * Sx;
-              const double Dy = E[1][ya][yb][1] + (P[1] - O[1]) * Sy;
-              const double Dz = E[2][za][zb][1] + (P[2] - O[2]) * Sz;
-              accM[0][x] += nab * s3 * Dx * Sy * Sz;
-              accM[1][x] += nab * s3 * Sx * Dy * Sz;
-              accM[2][x] += nab * s3 * Sx * Sy * Dz;
-            }
-        }
-      // nuclear attraction
+          }
+      }
+      // nuclear attraction of this thread's nucleus
       const int L = la + lb;
-      for (int at = a.atom_begin[m]; at < a.atom_end[m]; ++at) {
+      for (int at = atom; at <= atom; ++at) {
         const double C[3] = {a.atom_xyz[3 * at], a.atom_xyz[3 * at + 1], a.atom_xyz[3 * at + 2]};
         double R[125];
         const double X = P[0] - C[0], Y = P[1] - C[1], Z = P[2] - C[2];
@@ -1482,19 +1490,22 @@ __global__ void k_one_electron(OneEArgs a) {
           }
       }
     }
-  // scatter (each function pair belongs to exactly one shell pair)
+  // scatter (each function pair belongs to exactly one shell pair); V adds this
+  // nucleus's share to the zeroed matrix
   int x = 0;
   for (int ca = 0; ca < na; ++ca)
     for (int cb = 0; cb < nb; ++cb, ++x) {
       const int i = a.func[sa * kMaxComp + ca], j = a.func[sb * kMaxComp + cb];
       if (i < 0 || j < 0) continue;
+      if (sa == sb && cb > ca) continue;  // (ca, cb) already wrote both V[i][j] and V[j][i]
       const long long ij = base + (long long)i * N + j, ji = base + (long long)j * N + i;
+      atomicAdd(a.V + ij, accV[x]);
+      if (ji != ij) atomicAdd(a.V + ji, accV[x]);
+      if (!first) continue;
       a.S[ij] = accS[x];
       a.S[ji] = accS[x];
       a.T[ij] = accT[x];
       a.T[ji] = accT[x];
-      a.V[ij] = accV[x];
-      a.V[ji] = accV[x];
       for (int d = 0; d < 3; ++d) {
         a.M[d * a.nn + ij] = accM[d][x];
         a.M[d * a.nn + ji] = accM[d][x];
@@ -1557,7 +1568,9 @@ extern "C" int mmdg_one_electron(mmdg_context* h, int natom, const int* atom_mol
   a.T = T;
   a.V = V;
   a.M = M;
-  k_one_electron<<<(h->npair + 63) / 64, 64, 0, st>>>(a);
+  int max_atoms = 1;
+  for (int m = 0; m < h->nmol; ++m) max_atoms = std::max(max_atoms, ae[m] - ab[m]);
+  k_one_electron<<<dim3((h->npair + 63) / 64, max_atoms), 64, 0, st>>>(a);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(st));  // the temporary atom buffers are freed on return
   return MMDG_OK;

@@ -484,10 +484,6 @@ def generate_instances(outdir, ngroups=6):
             else:
                 inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<double>, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
                 inits.append(f"  if ((e = cudaFuncSetAttribute(k_fock<{md}<float>, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<float>, float>()))) return e;")
-                inits.append("#ifdef MMDG_EXP_CARVEOUT_L1")
-                for real in ("double", "float"):
-                    inits.append(f"  if (!{md}<{real}>::RSMEM && (e = cudaFuncSetAttribute(k_fock<{md}<{real}>, {real}>, cudaFuncAttributePreferredSharedMemoryCarveout, 0))) return e;")
-                inits.append("#endif")
             inits.append(f"  if ((e = cudaFuncSetAttribute(k_tensor<{md}<double>>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<{md}<double>, double>()))) return e;")
             if c[:2] == c[2:]:
                 t.append(f"cudaError_t launch_schwarz_{s}(const Geometry& g, const SchwarzArgs& a, const int* list, int n, cudaStream_t st) {{")

@@ -117,15 +117,6 @@ __device__ __forceinline__ double boys_row(const double2& c01, const double2& c2
 // 1/32 + 2^-17.
 template <int L>
 __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double T, double* Fn) {
-#ifdef MMDG_EXP_BOYS_MAGIC
-  if (T < kBoysTaylorMax) {
-    constexpr double kRound = 6755399441055744.0;
-    const double r = fma(T, 16.0, kRound);
-    const int k = __double2loint(r);
-    const double y = fma(r - kRound, 0.0625, -T);
-    const double2* __restrict__ c = reinterpret_cast<const double2*>(tab + (L * kBoysNGrid + k) * kBoysRow);
-    const double2 c01 = __ldg(c), c23 = __ldg(c + 1), c45 = __ldg(c + 2), c67 = __ldg(c + 3);
-#else
   const float Tf = f32_of_nonneg(T);
   if (Tf < float(kBoysTaylorMax)) {
     const int k = __float2int_rn(Tf * 16.0f);
@@ -133,7 +124,6 @@ __device__ __forceinline__ void boys_eval(const double* __restrict__ tab, double
     const double2* __restrict__ c = reinterpret_cast<const double2*>(tab + (L * kBoysNGrid + k) * kBoysRow);
     const double2 c01 = __ldg(c), c23 = __ldg(c + 1), c45 = __ldg(c + 2), c67 = __ldg(c + 3);
     const double y = c67.y - T;  // T_k - T
-#endif
     Fn[L] = boys_row(c01, c23, c45, c67, y);
     if (L == 1) {
       // F_0 from its own row: 6 FMAs instead of exp(-T) (7) and one recursion step (3)

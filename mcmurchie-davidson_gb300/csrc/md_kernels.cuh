@@ -128,7 +128,7 @@ constexpr int kMaxKeys = 256;
 
 // Evaluation of a bucketed quartet list: persistent grid-stride loop over
 // (chunk, bucket, quartet), chunk-major, so that a warp shares its chunk (code
-// path) and, inside a bucket, its primitive trip counts.
+// path) and, inside a bucket, its primitive trip counts; heaviest buckets first.
 template <class MD, typename Real>
 __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
                                                    const unsigned* count, const long long* key_off, int nkeys) {
@@ -153,7 +153,9 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
   for (long long idx = blockIdx.x * (long long)kThreads + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * kThreads) {
     const int chunk = (int)(idx / n);
-    const unsigned r = (unsigned)(idx - (long long)chunk * n);
+    // buckets run from the heaviest (most primitive pairs, stored last) to the
+    // lightest, so the persistent loop's last round holds the cheapest quartets
+    const unsigned r = n - 1u - (unsigned)(idx - (long long)chunk * n);
     if (r < s_pre[key]) key = 0;
     while (r >= s_pre[key + 1]) ++key;
     const int2 e = list[s_off[key] + (r - s_pre[key])];

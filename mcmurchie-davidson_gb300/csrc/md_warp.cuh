@@ -33,7 +33,7 @@
 namespace mmdg {
 
 constexpr int kWarps = kThreads / 32;
-constexpr int kItem = 8;  // list quartets per warp work item (k_fock_warp)
+constexpr int kItem = 8;  // most list quartets per warp work item (k_fock_warp)
 
 __device__ __forceinline__ int herm_index(int t, int u, int v) {
   const int n = t + u + v, m = n - t;
@@ -97,11 +97,15 @@ __global__ void __launch_bounds__(kThreads) k_fock_warp(Geometry g, FockArgs f, 
   // counts).  Their primitive quartets are grouped into batches of at most 32, whose
   // Boys functions the lanes evaluate together; a quartet with more than 32 primitive
   // quartets is evaluated alone, 32 at a time.
-  for (unsigned q0 = (blockIdx.x * kWarps + warp) * kItem; q0 < n; q0 += gridDim.x * kWarps * kItem) {
-    const int nq = (int)min((unsigned)kItem, n - q0);
+  // quartets per work item: up to kItem, fewer when the class has too few quartets
+  // to give every warp of the grid several items
+  const unsigned nwarps = gridDim.x * kWarps;
+  const int item = (int)max(1u, min((unsigned)kItem, n / (4u * nwarps)));
+  for (unsigned q0 = (blockIdx.x * kWarps + warp) * item; q0 < n; q0 += nwarps * item) {
+    const int nq = (int)min((unsigned)item, n - q0);
     int qbp = 0, qkp = 0, qnp = 0;  // lane x < nq: quartet x of the item
     if (lane < nq) {
-      const unsigned qi = q0 + lane;
+      const unsigned qi = n - 1u - (q0 + lane);  // heaviest buckets (stored last) first
       int key = 0;
       while (qi >= s_pre[key + 1]) ++key;
       const int2 e = list[s_off[key] + (qi - s_pre[key])];
