@@ -310,7 +310,10 @@ def batched_bench(nmol=1024, reps=5, sample_per_molecule=128, seed=3, parity_sam
             "per_molecule_fock_builds_per_s": rate_single,
             "per_molecule_sample": int(len(idx)),
             "speedup": (nmol / t_b) / rate_single,
-            "tuning": {"streams": tun.streams, "grids": tun.grids},
+            "tuning": {"streams": tun.streams, "grids": tun.grids, "tiles": tun.tiles,
+                       "build_ms_by_streams": tun.measured.get("build_ms_by_streams"),
+                       "class_ms_by_tile": {k: {"tiles": v["tiles"], "total_ms": float(np.sum(v["class_ms"]))}
+                                            for k, v in (tun.measured.get("class_ms_by_tile") or {}).items()}},
             "scf_time_s": t_scf, "scf_fock_launches": int(br.fock_builds),
             "converged": int(br.converged.sum()), "setup_s": t_setup,
             "mean_energy": float(np.mean(E)),

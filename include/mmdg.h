@@ -176,6 +176,12 @@ long long mmdg_boys_table(double* out, long long n);
  * occupancy); mmdg_set_streams spreads the classes (screening and evaluation) over
  * 1..8 concurrent streams (fork/join on events). */
 int mmdg_set_tuning(mmdg_context* ctx, int cls, int grid_blocks);
+/* Tile of class `cls`'s Fock kernel (no counterpart in the reference): threads per
+ * block of the one-thread-per-quartet kernels (64, 128 or 256; the classes whose
+ * Hermite tables live in shared memory keep 128) and the largest number of list
+ * quartets a warp takes per work item in the warp-cooperative high-L kernels (1..8,
+ * whose Boys functions are evaluated together); 0 restores the default. */
+int mmdg_set_tile(mmdg_context* ctx, int cls, int block_threads, int item);
 int mmdg_set_streams(mmdg_context* ctx, int nstreams);
 
 /* Primitive-pair screening of the next mmdg_set_basis (no counterpart in the

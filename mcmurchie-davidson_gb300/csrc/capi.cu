@@ -230,6 +230,8 @@ struct mmdg_context {
   DevBuf<long long> d_mol_shell0;
   // tuning (autotuner): persistent grid per class (0 = occupancy), concurrent class streams
   int class_grid[MMDG_NCLASS] = {0};
+  int class_block[MMDG_NCLASS] = {0};  // threads per block of the per-thread kernels (0: 128)
+  int class_item[MMDG_NCLASS] = {0};   // quartets per work item of the warp kernels (0: adaptive up to 8)
   int nstreams = 1;
   cudaStream_t side[kMaxStreams] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kMaxStreams] = {};
@@ -1128,11 +1130,12 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
       ClassLaunch cl{h->d_cls[cb].p, h->d_cls[ck].p, h->cls_count[cb], h->cls_count[ck], cb == ck, 0.f, split,
                      h->d_cls_moff[ck].p};
       const long long* ko = h->d_keyoff.p + h->kbase[ci];
-      const int grid = h->class_grid[ci];
-      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], grid, cs));
+      const int grid = h->class_grid[ci], blk = h->class_block[ci], item = h->class_item[ci];
+      CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], grid, blk,
+                      item, cs));
       if (split > 0.f)
         CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + h->total_keys + h->kbase[ci], ko,
-                        h->nkeys[ci], grid, cs));
+                        h->nkeys[ci], grid, blk, item, cs));
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;
@@ -1726,6 +1729,24 @@ extern "C" int mmdg_set_tuning(mmdg_context* h, int cls, int grid_blocks) {
   if (!h) return fail(MMDG_E_ARG, "mmdg_set_tuning: null context");
   if (cls < 0 || cls >= MMDG_NCLASS || grid_blocks < 0) return fail(MMDG_E_ARG, "mmdg_set_tuning: bad class or grid");
   h->class_grid[cls] = grid_blocks;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return MMDG_OK;
+}
+
+// tile of a class's Fock kernel: threads per block of the per-thread kernels (64, 128
+// or 256; classes with shared-memory R tables keep 128) and quartets per work item
+// of the warp-cooperative kernels (1..8); 0 restores the default
+extern "C" int mmdg_set_tile(mmdg_context* h, int cls, int block_threads, int item) {
+  if (!h) return fail(MMDG_E_ARG, "mmdg_set_tile: null context");
+  if (cls < 0 || cls >= MMDG_NCLASS) return fail(MMDG_E_ARG, "mmdg_set_tile: bad class");
+  if (block_threads != 0 && block_threads != 64 && block_threads != 128 && block_threads != 256)
+    return fail(MMDG_E_ARG, "mmdg_set_tile: threads per block must be 64, 128 or 256 (0: default)");
+  if (item < 0 || item > 8) return fail(MMDG_E_ARG, "mmdg_set_tile: quartets per work item must be 0..8");
+  h->class_block[cls] = block_threads;
+  h->class_item[cls] = item;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;

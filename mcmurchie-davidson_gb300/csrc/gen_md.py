@@ -422,7 +422,7 @@ def generate_instances(outdir, ngroups=6):
     files = []
     decl = ["// Generated by gen_md.py -- do not edit.", "#pragma once", '#include "md_kernels.cuh"',
             '#include "md_warp.cuh"', "namespace mmdg {",
-            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);",
+            "typedef cudaError_t (*fock_fn)(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, int, int, cudaStream_t);",
             "typedef cudaError_t (*tensor_fn)(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);",
             "typedef cudaError_t (*schwarz_fn)(const Geometry&, const SchwarzArgs&, const int*, int, cudaStream_t);",
             "typedef cudaError_t (*quartets_fn)(int, const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);",
@@ -431,7 +431,7 @@ def generate_instances(outdir, ngroups=6):
         decl.append(f"cudaError_t init_group{g}();")
     for c in cls:
         s = "".join(map(str, c))
-        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, cudaStream_t);")
+        decl.append(f"cudaError_t launch_fock_{s}(int, const Geometry&, const FockArgs&, const ClassLaunch&, const int2*, const unsigned*, const long long*, int, int, int, int, cudaStream_t);")
         decl.append(f"cudaError_t launch_tensor_{s}(const Geometry&, const TensorArgs&, const ClassLaunch&, cudaStream_t);")
         decl.append(f"cudaError_t launch_quartets_{s}(int, const Geometry&, const QuartetArgs&, const QuartetItem*, int, cudaStream_t);")
         if c[:2] == c[2:]:
@@ -452,16 +452,21 @@ def generate_instances(outdir, ngroups=6):
         for c in grp:
             s = "".join(map(str, c))
             md = f"MD_{s}"
-            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, const long long* koff, int nkeys, int grid, cudaStream_t st) {{")
+            t.append(f"cudaError_t launch_fock_{s}(int prec, const Geometry& g, const FockArgs& f, const ClassLaunch& cl, const int2* list, const unsigned* count, const long long* koff, int nkeys, int grid, int block, int item, cudaStream_t st) {{")
             if is_warp_class(c):
                 mw = f"MDW_{s}"
+                t.append("  (void)block;")
                 for real, cond in (("float", "if (prec)"), ("double", "else")):
                     k = f"k_fock_warp<{mw}<{real}>, {real}>"
                     sm = f"WarpSmem<{mw}<{real}>, {real}>::bytes()"
-                    t.append(f"  {cond} {k}<<<persistent_blocks({k}, {sm}, grid), kThreads, {sm}, st>>>(g, f, cl, list, count, koff, nkeys);")
+                    t.append(f"  {cond} {k}<<<persistent_blocks({k}, {sm}, grid), kThreads, {sm}, st>>>(g, f, cl, list, count, koff, nkeys, item);")
             else:
-                t.append(f"  if (prec) k_fock<{md}<float>, float><<<persistent_blocks(k_fock<{md}<float>, float>, smem_bytes<{md}<float>, float>(), grid), kThreads, smem_bytes<{md}<float>, float>(), st>>>(g, f, cl, list, count, koff, nkeys);")
-                t.append(f"  else k_fock<{md}<double>, double><<<persistent_blocks(k_fock<{md}<double>, double>, smem_bytes<{md}<double>, double>(), grid), kThreads, smem_bytes<{md}<double>, double>(), st>>>(g, f, cl, list, count, koff, nkeys);")
+                t.append("  (void)item;")
+                t.append(f"  if ({md}<double>::RSMEM || block <= 0) block = kThreads;  // shared-memory R tables are sized for kThreads")
+                for real, cond in (("float", "if (prec)"), ("double", "else")):
+                    k = f"k_fock<{md}<{real}>, {real}>"
+                    sm = f"smem_bytes<{md}<{real}>, {real}>()"
+                    t.append(f"  {cond} {k}<<<persistent_blocks({k}, {sm}, grid, block), block, {sm}, st>>>(g, f, cl, list, count, koff, nkeys);")
             t.append(f"  return cudaGetLastError();")
             t.append("}")
             t.append(f"cudaError_t launch_tensor_{s}(const Geometry& g, const TensorArgs& a, const ClassLaunch& cl, cudaStream_t st) {{")

@@ -15,7 +15,8 @@
 
 namespace mmdg {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 128;     // threads per block (shared-memory R tables are sized for it)
+constexpr int kMaxFockBlock = 256; // largest block a k_fock launch may use (autotuned tile)
 
 struct ClassLaunch {
   const int* bra;   // shell-pair indices of the bra class list
@@ -130,7 +131,7 @@ constexpr int kMaxKeys = 256;
 // (chunk, bucket, quartet), chunk-major, so that a warp shares its chunk (code
 // path) and, inside a bucket, its primitive trip counts; heaviest buckets first.
 template <class MD, typename Real>
-__global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
+__global__ void __launch_bounds__(kMaxFockBlock) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
                                                    const unsigned* count, const long long* key_off, int nkeys) {
   __shared__ unsigned s_pre[kMaxKeys + 1];
   __shared__ long long s_off[kMaxKeys];
@@ -150,8 +151,9 @@ __global__ void __launch_bounds__(kThreads) k_fock(Geometry g, FockArgs f, Class
   Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
   unsigned nfq = 0, nsq = 0, npq = 0, nbp = 0, nas = 0;
   int key = 0;
-  for (long long idx = blockIdx.x * (long long)kThreads + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * kThreads) {
+  // block size: kThreads for classes with shared-memory R tables, else 64..256 (tile)
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
     const int chunk = (int)(idx / n);
     // buckets run from the heaviest (most primitive pairs, stored last) to the
     // lightest, so the persistent loop's last round holds the cheapest quartets
@@ -253,11 +255,11 @@ namespace mmdg {
 // blocks of a persistent launch: every SM filled to the kernel's occupancy
 // (grid > 0: an autotuned grid, capped at that occupancy)
 template <typename K>
-inline int persistent_blocks(K kernel, size_t smem, int grid = 0) {
+inline int persistent_blocks(K kernel, size_t smem, int grid = 0, int block = kThreads) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem);
   const int full = sms * (per > 0 ? per : 1);
   return grid > 0 && grid < full ? grid : full;
 }

@@ -60,7 +60,7 @@ struct WarpSmem {
 template <class MD, typename Real>
 __global__ void __launch_bounds__(kThreads) k_fock_warp(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
                                                         const unsigned* count, const long long* key_off,
-                                                        int nkeys) {
+                                                        int nkeys, int max_item) {
   constexpr int L = MD::L, HL = MD::HL, HP = MD::HP, NAB = MD::NAB, NCD = MD::NCD;
   constexpr int NB = ncart(MD::LB), ND = ncart(MD::LD);
   constexpr int NKO = (NCD * HP + 31) / 32;  // ket-transform passes
@@ -100,7 +100,8 @@ __global__ void __launch_bounds__(kThreads) k_fock_warp(Geometry g, FockArgs f, 
   // quartets per work item: up to kItem, fewer when the class has too few quartets
   // to give every warp of the grid several items
   const unsigned nwarps = gridDim.x * kWarps;
-  const int item = (int)max(1u, min((unsigned)kItem, n / (4u * nwarps)));
+  const unsigned cap = max_item > 0 ? (unsigned)max_item : (unsigned)kItem;  // autotuned, or kItem
+  const int item = (int)max(1u, min(cap, n / (4u * nwarps)));
   for (unsigned q0 = (blockIdx.x * kWarps + warp) * item; q0 < n; q0 += nwarps * item) {
     const int nq = (int)min((unsigned)item, n - q0);
     int qbp = 0, qkp = 0, qnp = 0;  // lane x < nq: quartet x of the item

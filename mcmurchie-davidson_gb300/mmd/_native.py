@@ -47,6 +47,7 @@ def _bind(L):
         "mmdg_one_electron": (c_int, [p, c_int, p, p, p, p, p, p, p, p, p]),
         "mmdg_set_tuning": (c_int, [p, c_int, c_int]),
         "mmdg_set_streams": (c_int, [p, c_int]),
+        "mmdg_set_tile": (c_int, [p, c_int, c_int, c_int]),
         "mmdg_set_prim_tol": (c_int, [p, ctypes.c_double]),
         "mmdg_rhf_gradient": (c_int, [p, p, p, c_int, p, p, p, c_d, p, p]),
         "mmdg_fock_graph": (c_int, [p, p, p, c_d, c_d, p]),

@@ -8,7 +8,12 @@ Tunables (C ABI ``mmdg_set_tuning`` / ``mmdg_set_streams``):
 * the number of concurrent streams the 21 classes (screening and evaluation) are
   spread over (1, 2, 4, 8): one class at a time leaves the GPU idle in the small
   classes and in every kernel's tail;
-* with several streams, one grid size for all classes, timed as whole builds.
+* with several streams, one grid size for all classes, timed as whole builds;
+* per angular class, the tile of its evaluation kernel (``mmdg_set_tile``): threads
+  per block {64, 128, 256} of the one-thread-per-quartet kernels (classes whose
+  Hermite tables live in shared memory keep 128), quartets per warp work item
+  {1, 2, 4, 8} of the warp-cooperative high-L kernels (whose Boys functions are
+  evaluated together).
 
 Each candidate is timed with CUDA events on a representative density difference
 (``mmdg_fock_timed`` per class for the per-class grids, whole builds otherwise).
@@ -28,22 +33,33 @@ from . import _native
 CACHE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "_build", "tuning.json")
 
 
-class Tuning:
-    """A launch schedule: per-class persistent grid (0 = one full wave) and the number
-    of concurrent class streams."""
+BLOCKS = (64, 128, 256)   # threads per block, one-thread-per-quartet kernels
+ITEMS = (1, 2, 4, 8)      # quartets per warp work item, warp-cooperative kernels
 
-    def __init__(self, grids=None, streams=1, measured=None):
+
+class Tuning:
+    """A launch schedule: per-class persistent grid (0 = one full wave), per-class tile
+    (threads per block or quartets per warp item; 0 = default) and the number of
+    concurrent class streams."""
+
+    def __init__(self, grids=None, streams=1, measured=None, tiles=None):
         self.grids = list(grids) if grids is not None else [0] * _native.NCLASS
+        self.tiles = list(tiles) if tiles is not None else [0] * _native.NCLASS
         self.streams = int(streams)
         self.measured = measured or {}
 
     def apply(self, ctx):
+        from .flop_model import CLASSES, fock_kernel
         for c, g in enumerate(self.grids):
             _native.check(_native.lib().mmdg_set_tuning(ctx._h, c, int(g)), "mmdg_set_tuning")
+            warp = fock_kernel(CLASSES[c]) == "warp"
+            t = int(self.tiles[c])
+            _native.check(_native.lib().mmdg_set_tile(ctx._h, c, 0 if warp else t, t if warp else 0),
+                          "mmdg_set_tile")
         _native.check(_native.lib().mmdg_set_streams(ctx._h, self.streams), "mmdg_set_streams")
 
     def to_json(self):
-        return {"grids": self.grids, "streams": self.streams, "measured": self.measured}
+        return {"grids": self.grids, "tiles": self.tiles, "streams": self.streams, "measured": self.measured}
 
 
 def _key(ctx, fp32_below=0.0):
@@ -91,7 +107,7 @@ def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuni
     if use_cache:
         t = _load_cache().get(key)
         if t is not None:
-            tun = Tuning(t["grids"], t["streams"], t.get("measured"))
+            tun = Tuning(t["grids"], t["streams"], t.get("measured"), t.get("tiles"))
             tun.apply(ctx)
             return tun
     torch = ctx.torch
@@ -113,10 +129,30 @@ def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuni
             if acc[c] < best[c] * 0.98:  # prefer the default unless clearly better
                 best[c] = acc[c]
                 grids[c] = g
+    # tiles, one class at a time on one stream (with the grids chosen above)
+    from .flop_model import CLASSES, fock_kernel
+    warp = np.array([fock_kernel(c) == "warp" for c in CLASSES])
+    tiles = [0] * _native.NCLASS
+    best_tile = best.copy()
+    tile_ms = {}
+    for k in range(len(ITEMS)):
+        cand = [ITEMS[k] if w else (BLOCKS[k] if k < len(BLOCKS) else 0) for w in warp]
+        Tuning(grids, 1, tiles=cand).apply(ctx)
+        ctx.fock_timed(dP, tol=tol, fp32_below=fp32_below)  # warm
+        acc = np.zeros(_native.NCLASS)
+        for _ in range(reps):
+            _, ms, _ = ctx.fock_timed(dP, tol=tol, fp32_below=fp32_below)
+            acc += ms
+        acc /= reps
+        tile_ms[str(k)] = {"tiles": cand, "class_ms": acc.tolist()}
+        for c in range(_native.NCLASS):
+            if cand[c] and acc[c] < best_tile[c] * 0.98:
+                best_tile[c] = acc[c]
+                tiles[c] = cand[c]
     stream_ms = {}
     best_s, best_t = 1, np.inf
     for s in (1, 2, 4, 8):
-        Tuning(grids, s).apply(ctx)
+        Tuning(grids, s, tiles=tiles).apply(ctx)
         t = _time_build(ctx, dP, tol, fp32_below, reps)
         stream_ms[str(s)] = t * 1e3
         if t < best_t * 0.98:
@@ -126,13 +162,14 @@ def autotune(ctx, dP, tol=1e-12, fp32_below=0.0, reps=3, use_cache=True) -> Tuni
     grid_ms = {}
     if best_s > 1:
         for g in candidates:
-            Tuning([g] * _native.NCLASS, best_s).apply(ctx)
+            Tuning([g] * _native.NCLASS, best_s, tiles=tiles).apply(ctx)
             t = _time_build(ctx, dP, tol, fp32_below, reps)
             grid_ms[str(g)] = t * 1e3
             if t < best_t * 0.98:
                 grids, best_t = [g] * _native.NCLASS, t
-    tun = Tuning(grids, best_s, {"class_ms_by_grid": per, "build_ms_by_streams": stream_ms,
-                                 "build_ms_by_grid_with_streams": grid_ms})
+    tun = Tuning(grids, best_s, {"class_ms_by_grid": per, "class_ms_by_tile": tile_ms,
+                                 "build_ms_by_streams": stream_ms,
+                                 "build_ms_by_grid_with_streams": grid_ms}, tiles=tiles)
     tun.apply(ctx)
     if use_cache:
         _store_cache(key, tun)

@@ -70,3 +70,30 @@ def test_batched_rhf_energies_match_single_molecule_rhf():
         m = Molecule(g, "6-31g")
         e1 = m.RHF(doPrint=False, direct=True, conver=1e-10)
         assert abs(e - e1) < 1e-10, (e, e1)
+
+
+def test_every_tile_gives_the_same_fock_build():
+    """mmdg_set_tile: 64/128/256 threads per block for the one-thread-per-quartet
+    kernels and 1..8 quartets per warp work item for the high-L kernels change the
+    schedule, not the result (water 6-31G**: every class present)."""
+    import torch
+    from mmd import _native, autotune
+    from mmd.flop_model import CLASSES, fock_kernel
+    from mmd.molecule import Molecule
+    mol = Molecule("\n0 1\nO 0.0 -0.075791844 0.0\nH 0.866811829 0.601435779 0.0\nH -0.866811829 0.601435779 0.0\n",
+                   "6-31gss")
+    ctx = mol.context
+    rng = np.random.default_rng(8)
+    A = rng.standard_normal((mol.nbasis, mol.nbasis))
+    dP = torch.tensor((A + A.T).ravel(), device="cuda")
+    ref = ctx.fock(dP, tol=1e-12).clone()
+    warp = [fock_kernel(c) == "warp" for c in CLASSES]
+    try:
+        for k in range(4):
+            tiles = [autotune.ITEMS[k] if w else (autotune.BLOCKS[k] if k < 3 else 0) for w in warp]
+            autotune.Tuning(tiles=tiles, streams=1).apply(ctx)
+            assert torch.max(torch.abs(ctx.fock(dP, tol=1e-12) - ref)).item() < 1e-12, tiles
+    finally:
+        autotune.Tuning(streams=_native.DEFAULT_STREAMS_SINGLE).apply(ctx)
+    with pytest.raises(_native.MMDGError):
+        _native.check(_native.lib().mmdg_set_tile(ctx._h, 0, 96, 0), "mmdg_set_tile")
