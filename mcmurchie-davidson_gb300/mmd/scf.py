@@ -37,23 +37,14 @@ import numpy as np
 HOST_EIGH_MAX_N = 1024
 
 
-def host_eigh(A, nlow=None):
+def host_eigh(A):
     """One symmetric eigensolve on the host cores: LAPACK dsyevd through SciPy (on the
     16-core Grace CPU 0.64 ms at N = 104 against 2.8 ms for numpy.linalg.eigh; 7.4 ms at
-    N = 400 and 28 ms at N = 800, where cuSOLVER's syevd takes 11.8 and 31 ms).  With
-    ``nlow``, only the lowest ``nlow`` eigenpairs (LAPACK dsyevr on that index range):
-    what an SCF iteration needs for its density.  Many small solves at once (the
-    batched SCF) stay on numpy.linalg.eigh in a thread pool: SciPy's wrapper serialises
-    there (1.14 s against 0.45 s for 1024 matrices)."""
+    N = 400 and 28 ms at N = 800, where cuSOLVER's syevd takes 11.8 and 31 ms).  Many
+    small solves at once (the batched SCF) stay on numpy.linalg.eigh in a thread pool:
+    SciPy's wrapper serialises there (1.14 s against 0.45 s for 1024 matrices)."""
     import scipy.linalg
-    if nlow is not None and 0 < nlow < A.shape[0]:
-        return scipy.linalg.eigh(A, driver="evr", subset_by_index=[0, nlow - 1], check_finite=False)
     return scipy.linalg.eigh(A, driver="evd", check_finite=False)
-
-
-# SCF iterations solve for the occupied orbitals only (the density needs no more);
-# the full orbital set is solved once, for the converged Fock matrix
-HOST_EIGH_OCCUPIED = True
 
 
 # an initial guess is abandoned (restart from the core guess) when the DIIS error
@@ -367,9 +358,9 @@ class _RHFState:
             self.FO = X.T @ self.F @ X
         if self.FO.shape[0] <= HOST_EIGH_MAX_N:
             # up to ~1000 functions LAPACK on the host cores beats cuSOLVER's syevd
-            w, v = host_eigh(self.FO.cpu().numpy(), mol.nocc if HOST_EIGH_OCCUPIED else None)
+            w, v = host_eigh(self.FO.cpu().numpy())
             E = torch.from_numpy(w).to(self.FO.device)
-            CO = torch.from_numpy(np.ascontiguousarray(v)).to(self.FO.device)
+            CO = torch.from_numpy(v).to(self.FO.device)
         else:
             E, CO = torch.linalg.eigh(self.FO)
         self.E, self.CO = E, CO
@@ -384,15 +375,8 @@ class _RHFState:
         self.step += 1
 
     def finish(self):
-        """Results back to the reference's attribute names (host arrays); the full
-        orbital set of the last orthogonalised Fock matrix when the iterations solved
-        for the occupied orbitals only."""
+        """Results back to the reference's attribute names (host arrays)."""
         mol = self.mol
-        if self.CO.shape[1] < self.CO.shape[0]:
-            w, v = host_eigh(self.FO.cpu().numpy())
-            self.E = self.torch.from_numpy(w).to(self.FO.device)
-            self.CO = self.torch.from_numpy(v).to(self.FO.device)
-            self.C = self.X @ self.CO
         mol.P = self.P.cpu().numpy()
         mol.P_old = self.P_old.cpu().numpy()
         mol.F = self.F.cpu().numpy()
