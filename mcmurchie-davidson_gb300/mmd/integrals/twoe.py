@@ -69,8 +69,10 @@ class Basis:
 # Device contexts by basis fingerprint, least recently used first.  The cache is
 # bounded by the device bytes its contexts hold (a context's quartet lists grow as
 # S^4/8 in the number of shells: 1.4 GB for (H2O)16 6-31G**, 22 GB for (H2O)32) and
-# by a count; the oldest contexts are released first.  MMD_CONTEXT_CACHE_BYTES
-# overrides the byte budget.
+# by a count; the oldest entries are dropped first.  Dropping an entry releases only
+# the cache's reference: a context still held by a Molecule stays valid and frees its
+# device memory when its last holder lets go.  MMD_CONTEXT_CACHE_BYTES overrides the
+# byte budget.
 _ctx_cache: "OrderedDict" = OrderedDict()
 CONTEXT_CACHE_MAX = 16
 CONTEXT_CACHE_BYTES = int(float(os.environ.get("MMD_CONTEXT_CACHE_BYTES", 48e9)))
@@ -89,9 +91,8 @@ def _trim_cache(keep=None):
                 break
             _ctx_cache.move_to_end(k)
             continue
-        c = _ctx_cache.pop(k)
+        _ctx_cache.pop(k)
         total -= sizes.pop(k)
-        c.close()
 
 
 def context_for(bfs):
@@ -108,9 +109,8 @@ def context_for(bfs):
 
 
 def clear_context_cache():
-    """Release every cached device context."""
-    while _ctx_cache:
-        _ctx_cache.popitem(last=False)[1].close()
+    """Drop every cached device context (contexts still held elsewhere stay valid)."""
+    _ctx_cache.clear()
 
 
 def ERI(a, b, c, d) -> float:

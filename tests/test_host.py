@@ -286,3 +286,29 @@ def test_issued_and_useful_flop_counts():
     assert F.boys_flops(3, True) < F.boys_flops(3, False)
     # the recursion counts 1 FLOP for a first step and 3 for fma(X, R1, (m-1) R2)
     assert F.recursion_flops(1) == 3 and F.recursion_flops(2) == 3 + 6 * 1 + 3 * 3
+
+
+def test_context_cache_eviction_keeps_held_contexts_open(monkeypatch):
+    """Dropping a cache entry must not close a context a Molecule still uses."""
+    from mmd.integrals import twoe
+
+    class FakeCtx:
+        closed = False
+
+        def device_bytes(self):
+            return 10
+
+        def close(self):
+            self.closed = True
+
+    monkeypatch.setattr(twoe, "CONTEXT_CACHE_MAX", 2)
+    twoe._ctx_cache.clear()
+    held = []
+    for k in range(4):
+        c = FakeCtx()
+        held.append(c)
+        twoe._ctx_cache[("k", k)] = c
+        twoe._trim_cache(keep=("k", k))
+    assert len(twoe._ctx_cache) == 2 and not any(c.closed for c in held)
+    twoe.clear_context_cache()
+    assert not twoe._ctx_cache and not any(c.closed for c in held)
