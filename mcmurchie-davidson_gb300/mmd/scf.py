@@ -375,14 +375,19 @@ class _RHFState:
         self.step += 1
 
     def finish(self):
-        """Results back to the reference's attribute names (host arrays)."""
+        """Results back to the reference's attribute names (host arrays), with the
+        reference's types: P, P_old, F, FO, C and CO complex128 (mmd/scf.py:15,24 start
+        them complex; the imaginary parts are zero for RHF), the orbital energies MO
+        real.  The energy stays a real float64 (the reference's carries a zero
+        imaginary part)."""
         mol = self.mol
-        mol.P = self.P.cpu().numpy()
-        mol.P_old = self.P_old.cpu().numpy()
-        mol.F = self.F.cpu().numpy()
-        mol.FO = self.FO.cpu().numpy()
-        mol.C = self.C.cpu().numpy()
-        mol.CO = self.CO.cpu().numpy()
+        cplx = lambda t: t.cpu().numpy().astype(np.complex128)
+        mol.P = cplx(self.P)
+        mol.P_old = cplx(self.P_old)
+        mol.F = cplx(self.F)
+        mol.FO = cplx(self.FO)
+        mol.C = cplx(self.C)
+        mol.CO = cplx(self.CO)
         mol.MO = self.E.cpu().numpy()
         mol.energy = np.float64(self.energy)
         mol.el_energy = mol.energy - mol.nuc_energy
