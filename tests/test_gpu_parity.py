@@ -281,7 +281,7 @@ def test_mixed_precision_fock_and_energy():
     assert abs(E32 - E64) < 1e-8, (E32, E64)
     # one full build on the converged density: max element error of G
     ctx = m64.context
-    P = torch.tensor(m64.P, device="cuda").reshape(-1).contiguous()
+    P = torch.tensor(np.real(m64.P), device="cuda").reshape(-1).contiguous()
     G64 = ctx.fock(P, tol=1e-12).clone()
     G32 = ctx.fock(P, tol=1e-12, fp32_below=1e-5)
     assert torch.max(torch.abs(G64 - G32)).item() < 1e-9
