@@ -198,11 +198,13 @@ class BatchRHF:
         Cocc = C * mask[:, None, :]
         return Cocc @ Cocc.transpose(1, 2)
 
-    def run(self, conver=1e-8, maxiter=100, DIIS=True, guess=None, guess_fallback=True, polish=False):
+    def run(self, conver=1e-8, maxiter=100, DIIS=True, guess=None, guess_fallback=True, polish=False,
+            polish_fp32_below=0.0):
         """RHF of every molecule; returns the energies (numpy, Eh).
 
-        ``polish``: after convergence, one non-incremental FP64 Fock build of the
-        converged densities and the energy E(P) = tr((H + F(P)) P) + E_nuc from it
+        ``polish``: after convergence, one non-incremental Fock build of the converged
+        densities (FP64, or FP32 below ``polish_fp32_below``) and the energy
+        E(P) = tr((H + F(P)) P) + E_nuc from it
         (returned; the SCF's own last energies stay in ``energies_raw``).  This
         removes what the incremental builds accumulate (screening drops, FP32
         quartets) from the energy and leaves only the density's own convergence
@@ -322,7 +324,7 @@ class BatchRHF:
         if polish:
             dP = self._pack(P)
             G = torch.empty_like(dP)
-            self.ctx.fock(dP, G, tol=self.acc2e, fp32_below=0.0)
+            self.ctx.fock(dP, G, tol=self.acc2e, fp32_below=float(polish_fp32_below))
             Gp = self._pad(G)
             Fp = Core + 0.5 * (Gp + Gp.transpose(1, 2))
             energy = (torch.sum((Core + Fp) * P.transpose(1, 2), dim=(1, 2))).cpu().numpy() + self.nuc
