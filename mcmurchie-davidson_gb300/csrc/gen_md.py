@@ -363,19 +363,25 @@ def gen_herm_tables():
     """Packed (t | u << 5 | v << 10) of every Hermite index, for each total L of the
     warp-cooperative classes."""
     out = []
-    for L in sorted({sum(c) for c in classes() if sum(c) > COMPACT_ABOVE_L}):
+    for L in sorted({sum(c) for c in classes() if is_warp_class(c)}):
         vals = [t | u << 5 | v << 10 for (t, u, v) in herm(L)]
         out.append(f"static __constant__ short kWH_{L}[{len(vals)}] = {{{', '.join(map(str, vals))}}};")
     return "\n".join(out)
 
 
 def is_warp_class(cl):
-    return sum(cl) > COMPACT_ABOVE_L
+    return sum(cl) > WARP_FOCK_ABOVE_L
 
 
-# classes with la+lb+lc+ld above this use the compact form (and, for Fock builds,
-# the warp-cooperative kernel of md_warp.cuh)
+# classes with la+lb+lc+ld above this use the compact form (k_tensor, k_quartets,
+# k_schwarz)
 COMPACT_ABOVE_L = 4
+# classes with la+lb+lc+ld above this run Fock builds in the warp-cooperative kernel
+# of md_warp.cuh, the others in the per-thread kernel k_fock.  Measured on (H2O)16
+# 6-31G** (ms per build, per-thread -> warp form): L = 4 (pp|pp) 2.31 -> 3.32,
+# (dp|pp) 3.30 -> 4.62, (dd|ss) 0.51 -> 1.16; L = 3 (pp|ps) 3.85 -> 7.69: below L = 5
+# the warp form's lane padding and recursion passes cost more than they save.
+WARP_FOCK_ABOVE_L = 4
 # register-resident classes up to this total L unroll the ket primitive loop by two
 UNROLL_KET_MAX_L = 2
 

@@ -146,8 +146,9 @@ def r0_flops(L: int, asymptotic: bool) -> int:
 
 @lru_cache(maxsize=None)
 def recursion_flops(L: int) -> int:
-    """The in-place Hermite Coulomb recursion of the per-thread code: X R1 (1 FLOP), or
-    fma(X, R1, (m-1) R2) (3 FLOPs) when the stepped index m exceeds 1."""
+    """The in-place Hermite Coulomb recursion of the per-thread code: X R1 (1 FLOP) when
+    the stepped index m is 1, fma(X, R1, R2) (2 FLOPs) when m = 2 (the factor m - 1 = 1
+    is folded), fma(X, R1, (m-1) R2) (3 FLOPs) when m > 2."""
     g = _gm()
     tot = 0
     for s in range(1, L + 1):
@@ -155,7 +156,7 @@ def recursion_flops(L: int) -> int:
             if (t, u, v) == (0, 0, 0):
                 continue
             m = t if t > 0 else (u if u > 0 else v)
-            tot += 3 if m > 1 else 1
+            tot += 3 if m > 2 else (2 if m == 2 else 1)
     return tot
 
 

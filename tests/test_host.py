@@ -284,8 +284,10 @@ def test_issued_and_useful_flop_counts():
     assert F.r0_flops(0, False) == 3 + 5 + 1 + 8 + 3 + 1 + 13 + 1
     assert F.useful_flops((0, 0, 0, 0), [1, 1, 1, 1, 0]) == F.r0_flops(0, False) + 2 + 2 + 6
     assert F.boys_flops(3, True) < F.boys_flops(3, False)
-    # the recursion counts 1 FLOP for a first step and 3 for fma(X, R1, (m-1) R2)
-    assert F.recursion_flops(1) == 3 and F.recursion_flops(2) == 3 + 6 * 1 + 3 * 3
+    # the recursion counts 1 FLOP for a first step, 2 for fma(X, R1, R2) (m = 2) and 3
+    # for fma(X, R1, (m-1) R2); level 3 has 10 entries with m = 1, 6 with m = 2, 3 with m = 3
+    assert F.recursion_flops(1) == 3 and F.recursion_flops(2) == 3 + 6 * 1 + 3 * 2
+    assert F.recursion_flops(3) == F.recursion_flops(2) + 10 * 1 + 6 * 2 + 3 * 3
 
 
 def test_context_cache_eviction_keeps_held_contexts_open(monkeypatch):
