@@ -47,6 +47,154 @@ def host_eigh(A):
     return scipy.linalg.eigh(A, driver="evd", check_finite=False)
 
 
+class OccupiedSubspace:
+    """The lowest ``nocc`` eigenpairs of the orthogonalised Fock matrix FO by
+    Chebyshev-filtered subspace iteration (Y. Zhou, Y. Saad, M. L. Tiago and J. R.
+    Chelikowsky, "Self-consistent-field calculations using Chebyshev-filtered subspace
+    iteration", J. Comput. Phys., 2006), warm-started from the previous SCF iteration's
+    Ritz vectors.
+
+    Between SCF iterations only the occupied orbitals are needed (P = C_occ C_occ^T);
+    a dense eigensolve of all N orbitals costs 7-10 ms on the host cores at N = 400,
+    one pass here a few dozen GEMMs of N x N x k on the GPU (k = nocc + a buffer) and
+    one k x k generalised eigensolve on the host.  One pass:
+
+    1. filters.  p_m(FO) with p_m the degree-m Chebyshev polynomial of the first kind
+       mapped onto [a, b] and scaled to 1 at the bottom of the slice (three-term
+       recurrence), b an upper bound of the spectrum -- the largest eigenvalue of the
+       last dense solve plus ||FO - FO_dense||_F (Weyl's inequality) -- and a the
+       cut-off below which the polynomial amplifies.  The occupied spectrum of a
+       molecule with heavy atoms is wide (O 1s near -20.6 Eh, the HOMO near -0.5 Eh),
+       and one polynomial would amplify the core ~1e12 times more than the HOMO, which
+       no Rayleigh-Ritz in FP64 recovers.  So the block is cut into two slices: the
+       core (Ritz values whose amplification exceeds the HOMO's by more than
+       ``spread``), filtered on [lowest valence value, b] with degree ``core_degree``,
+       and the valence + buffer, filtered on [top of the block, b] with degree
+       ``degree`` in the complement of the core (each product by FO is projected:
+       Z - V_c V_c^T Z);
+    2. Rayleigh-Ritz over both slices: columns normalised, H = Y^T FO Y and M = Y^T Y
+       solved on the host (H z = theta M z), V = Y Z;
+    3. residuals ||FO v - theta v|| of the occupied Ritz pairs; another pass while the
+       largest is above ``tol``.
+
+    After ``max_passes`` the caller falls back to the dense solve (``start`` again),
+    so a poor warm start (a guess reverted to the core guess) costs time, not
+    accuracy."""
+
+    def __init__(self, nocc: int, nbuf: int = 0, degree: int = 10, core_degree: int = 4, tol: float = 1e-8,
+                 max_passes: int = 4, spread: float = 1e3):
+        self.nocc = int(nocc)
+        self.k = int(nocc) + int(nbuf if nbuf > 0 else self.buffer(nocc))
+        self.degree = int(degree)
+        self.core_degree = int(core_degree)
+        self.tol = float(tol)
+        self.max_passes = int(max_passes)
+        self.log_spread = float(np.log(spread))
+        self.V = None
+        self.passes = 0
+        self.solves = 0
+        self.fallbacks = 0
+
+    @staticmethod
+    def buffer(nocc: int) -> int:
+        return max(8, nocc // 4)
+
+    @staticmethod
+    def applicable(n: int, nocc: int) -> bool:
+        return n >= 64 and nocc + OccupiedSubspace.buffer(nocc) <= n // 2
+
+    def start(self, FO, w, v):
+        """Warm start from a dense solve of FO (device matrix; host eigenpairs w, v)."""
+        import torch
+        self.V = torch.as_tensor(np.ascontiguousarray(v[:, : self.k]), device=FO.device)
+        self.theta = np.array(w[: self.k])
+        self.lmin, self.lmax = float(w[0]), float(w[-1])
+        self.F_dense = FO.clone()
+
+    @staticmethod
+    def _log_cheb(m, t):
+        """log |T_m(t)| for |t| >= 1 (0 inside [-1, 1], where |T_m| <= 1)."""
+        t = np.abs(np.asarray(t, dtype=float))
+        return np.where(t > 1.0, m * np.arccosh(np.maximum(t, 1.0)), 0.0)
+
+    def core_count(self, theta, a, b):
+        """Number of lowest Ritz values whose amplification by the valence filter
+        exceeds the HOMO's by more than the allowed spread."""
+        e, c = 0.5 * (b - a), 0.5 * (b + a)
+        lg = self._log_cheb(self.degree, (theta - c) / e)
+        over = lg[: self.nocc] - lg[self.nocc - 1] > self.log_spread
+        return int(np.argmin(over)) if not over.all() else 0
+
+    @staticmethod
+    def _filter(FO, X, a, b, lo, m, Vc=None):
+        """p_m(FO) X: Chebyshev filter on [a, b] scaled to 1 at ``lo`` (< a); products by
+        FO projected onto the complement of Vc's columns when given."""
+        import torch
+
+        def apply(Z):
+            FZ = FO @ Z
+            if Vc is not None:
+                FZ = FZ - Vc @ (Vc.T @ FZ)
+            return FZ
+
+        e, c = 0.5 * (b - a), 0.5 * (b + a)
+        sigma = e / (lo - c)
+        tau = 2.0 / sigma
+        Y = (apply(X) - c * X) * (sigma / e)
+        for _ in range(2, m + 1):
+            s1 = 1.0 / (tau - sigma)
+            Yn = apply(Y).sub_(Y, alpha=c).mul_(2.0 * s1 / e).sub_(X, alpha=sigma * s1)
+            X, Y, sigma = Y, Yn, s1
+        if Vc is not None:
+            Y = Y - Vc @ (Vc.T @ Y)
+        return Y
+
+    def solve(self, FO):
+        """(theta_occ on the host, V_occ on the device) of FO, or None when the passes
+        did not converge (then call ``start`` with a dense solve)."""
+        import scipy.linalg
+        import torch
+        if self.V is None:
+            return None
+        dF = float(torch.linalg.norm(FO - self.F_dense))
+        b = self.lmax + dF
+        lo = self.lmin - dF
+        V, theta = self.V, self.theta
+        for _ in range(self.max_passes):
+            self.passes += 1
+            a = float(theta[-1])
+            if not (lo < float(theta[0]) and a < b):
+                break
+            nc = self.core_count(theta, a, b)
+            if nc:
+                Vc = V[:, :nc]
+                Yc = self._filter(FO, Vc, float(theta[nc]), b, lo, self.core_degree)
+                Yv = self._filter(FO, V[:, nc:], a, b, float(theta[nc]) - dF, self.degree, Vc)
+                Y = torch.cat((Yc, Yv), dim=1)
+            else:
+                Y = self._filter(FO, V, a, b, lo, self.degree)
+            Y = Y / torch.linalg.norm(Y, dim=0)
+            FY = FO @ Y
+            HM = torch.stack((Y.T @ FY, Y.T @ Y)).cpu().numpy()
+            H = 0.5 * (HM[0] + HM[0].T)
+            M = 0.5 * (HM[1] + HM[1].T)
+            try:
+                theta, Z = scipy.linalg.eigh(H, M, check_finite=False)
+            except (np.linalg.LinAlgError, ValueError):
+                break
+            Zd = torch.as_tensor(Z, device=FO.device)
+            V = Y @ Zd
+            R = FY @ Zd[:, : self.nocc] - V[:, : self.nocc] * torch.as_tensor(theta[: self.nocc], device=FO.device)
+            res = float(torch.linalg.norm(R, dim=0).max())
+            if res < self.tol:
+                self.V, self.theta = V, theta
+                self.solves += 1
+                return theta[: self.nocc], V[:, : self.nocc]
+        self.fallbacks += 1
+        self.V = None
+        return None
+
+
 # an initial guess is abandoned (restart from the core guess) when the DIIS error
 # has grown this many iterations in a row
 GUESS_FALLBACK_GROWTH = 3
@@ -65,7 +213,8 @@ class SCF(object):
     """SCF methods for the molecule object (mmd/scf.py:8-180)."""
 
     def RHF(self, doPrint=True, DIIS=True, direct=False, conver=1e-8, acc2e=1e-12, fp32_below=0.0, guess=None,
-            guess_fallback=True, maxiter=100, polish=False, process_group=None, polish_fp32_below=0.0):
+            guess_fallback=True, maxiter=100, polish=False, process_group=None, polish_fp32_below=0.0,
+            eigensolver="dense"):
         """Restricted Hartree-Fock (mmd/scf.py:10-80): core-Hamiltonian start (or the
         density ``guess``, abandoned for the core guess after three growing DIIS
         errors when ``guess_fallback``), DIIS, stop on ||P - P_old||_F < conver.
@@ -74,9 +223,13 @@ class SCF(object):
         it in FP32; ``polish``: the returned energy from one non-incremental build of
         the final density (FP64, or FP32 below ``polish_fp32_below``), exact to second
         order in the density error -- a density converged to 1e-5 gives the energy to
-        ~1e-11 Eh.  Returns the energy (a numpy float64)."""
+        ~1e-11 Eh; ``eigensolver="subspace"``: the occupied orbitals of every iteration
+        after the first by Chebyshev-filtered subspace iteration on the GPU
+        (``OccupiedSubspace``, residuals below conver / 1000), the full set once at the
+        end.  Returns the energy (a numpy float64)."""
         state = self.scf_begin(DIIS=DIIS, direct=direct, acc2e=acc2e, fp32_below=fp32_below, guess=guess,
-                               guess_fallback=guess_fallback, maxiter=maxiter, process_group=process_group)
+                               guess_fallback=guess_fallback, maxiter=maxiter, process_group=process_group,
+                               eigensolver=eigensolver, subspace_tol=min(1e-8, max(1e-12, 1e-3 * conver)))
         t_start = time.perf_counter()
         for step in range(self.maxiter):
             state.iterate()
@@ -108,7 +261,7 @@ class SCF(object):
         return self.energy
 
     def scf_begin(self, DIIS=True, direct=False, acc2e=1e-12, fp32_below=0.0, guess=None, guess_fallback=True,
-                  maxiter=100, build=True, process_group=None):
+                  maxiter=100, build=True, process_group=None, eigensolver="dense", subspace_tol=1e-8):
         """Integrals and the initial state of an RHF run; returns the iteration object."""
         self.is_converged = False
         self.delta_energy = 1e20
@@ -122,7 +275,13 @@ class SCF(object):
         if build or not getattr(self, "is_built", False):
             self.build(self.direct)
         self._set_sharding(process_group if direct else None)
-        return _RHFState(self, DIIS, guess, guess_fallback)
+        if eigensolver not in ("dense", "subspace"):
+            raise ValueError("eigensolver must be 'dense' or 'subspace'")
+        sub = None
+        if eigensolver == "subspace" and OccupiedSubspace.applicable(self.nbasis, self.nocc):
+            sub = OccupiedSubspace(self.nocc, tol=subspace_tol)
+        self.subspace = sub
+        return _RHFState(self, DIIS, guess, guess_fallback, sub)
 
     def _set_sharding(self, group):
         """Sharded Fock builds over ``group`` (one GPU per rank), or none."""
@@ -297,8 +456,9 @@ class SCF(object):
 class _RHFState:
     """One RHF run on the device; ``iterate()`` is one pass of mmd/scf.py:30-60."""
 
-    def __init__(self, mol, DIIS, guess, guess_fallback):
+    def __init__(self, mol, DIIS, guess, guess_fallback, subspace=None):
         self.mol = mol
+        self.sub = subspace
         ctx = mol.context
         self.ctx = ctx
         torch = ctx.torch
@@ -358,18 +518,17 @@ class _RHFState:
                     self.fockSet.clear()
                     self.errorSet.clear()
                     self.FO = X.T @ self.F @ X
+                    if self.sub is not None:
+                        self.sub.V = None  # dense solve, then a fresh warm start
         if not self.DIIS or self.step == 0:
             self.FO = X.T @ self.F @ X
-        if self.FO.shape[0] <= HOST_EIGH_MAX_N:
-            # up to ~1000 functions LAPACK on the host cores beats cuSOLVER's syevd
-            w, v = host_eigh(self.FO.cpu().numpy())
-            E = torch.from_numpy(w).to(self.FO.device)
-            CO = torch.from_numpy(v).to(self.FO.device)
+        occ = self.sub.solve(self.FO) if self.sub is not None and self.step > 0 else None
+        if occ is not None:  # occupied orbitals only (subspace iteration)
+            self.E, self.CO, self.C = None, None, None
+            Cocc = X @ occ[1]
         else:
-            E, CO = torch.linalg.eigh(self.FO)
-        self.E, self.CO = E, CO
-        self.C = X @ CO
-        Cocc = self.C[:, : mol.nocc]
+            self._dense_solve()
+            Cocc = self.C[:, : mol.nocc]
         self.P = Cocc @ Cocc.T
         self.energy = float(torch.sum((Core + self.F) * self.P.T).item()) + mol.nuc_energy
         if self.step > 0:
@@ -378,6 +537,24 @@ class _RHFState:
         mol.energy = np.float64(self.energy)
         self.step += 1
 
+    def _dense_solve(self):
+        """All eigenpairs of FO (host LAPACK up to HOST_EIGH_MAX_N, cuSOLVER above);
+        restarts the subspace iteration's warm start when one is in use."""
+        torch = self.torch
+        if self.FO.shape[0] <= HOST_EIGH_MAX_N:
+            # up to ~1000 functions LAPACK on the host cores beats cuSOLVER's syevd
+            w, v = host_eigh(self.FO.cpu().numpy())
+            E = torch.from_numpy(w).to(self.FO.device)
+            CO = torch.from_numpy(v).to(self.FO.device)
+            if self.sub is not None:
+                self.sub.start(self.FO, w, v)
+        else:
+            E, CO = torch.linalg.eigh(self.FO)
+            if self.sub is not None:
+                self.sub.start(self.FO, E.cpu().numpy(), CO.cpu().numpy())
+        self.E, self.CO = E, CO
+        self.C = self.X @ CO
+
     def finish(self):
         """Results back to the reference's attribute names (host arrays), with the
         reference's types: P, P_old, F, FO, C and CO complex128 (mmd/scf.py:15,24 start
@@ -385,6 +562,8 @@ class _RHFState:
         real.  The energy stays a real float64 (the reference's carries a zero
         imaginary part)."""
         mol = self.mol
+        if self.E is None:  # the last iteration solved for the occupied orbitals only
+            self._dense_solve()
         cplx = lambda t: t.cpu().numpy().astype(np.complex128)
         mol.P = cplx(self.P)
         mol.P_old = cplx(self.P_old)

@@ -47,3 +47,31 @@ def test_combined_form_matches_the_reference_energies():
     assert br.converged.all()
     err = np.abs(np.asarray(E) - np.array([e for _, e in ref]))
     assert err.max() < 1e-8, err
+
+
+def test_chosen_single_molecule_form_matches_the_reference_energies():
+    """The single-molecule chosen form of the benchmark -- learned guess, FP32 below
+    Schwarz 1e-3, stop at ||dP|| < 1e-5, occupied orbitals by subspace iteration, polish
+    build (FP32 below 1e-7) -- against the reference's energies, and the same run with
+    the dense eigensolver within 1e-9 Eh of it."""
+    from mmd import guess as G
+    from mmd.clusters import water_cluster
+    from mmd.molecule import Molecule
+    net = G.DensityMLP.load()
+    for seed, e_ref in _reference()[:4]:
+        g = water_cluster(8, seed=seed)
+        out = {}
+        for eig in ("subspace", "dense"):
+            mol = Molecule(g, "6-31g")
+            P0 = G.predict_density(net, mol)
+            out[eig] = float(mol.RHF(doPrint=False, direct=True, fp32_below=1e-3, guess=P0, conver=1e-5, polish=True,
+                                     polish_fp32_below=1e-7, eigensolver=eig))
+            assert mol.is_converged
+            if eig == "subspace":
+                assert mol.subspace is not None and mol.subspace.solves > 0
+                # the full orbital set after the run, consistent with the final density
+                C = np.real(mol.C)[:, : mol.nocc]
+                assert mol.MO.shape == (mol.nbasis,)
+                assert np.abs(C @ C.T - np.real(mol.P)).max() < 1e-6
+        assert abs(out["subspace"] - e_ref) < 1e-8, (seed, out["subspace"] - e_ref)
+        assert abs(out["subspace"] - out["dense"]) < 1e-9, (seed, out["subspace"] - out["dense"])

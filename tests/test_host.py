@@ -314,3 +314,41 @@ def test_context_cache_eviction_keeps_held_contexts_open(monkeypatch):
     assert len(twoe._ctx_cache) == 2 and not any(c.closed for c in held)
     twoe.clear_context_cache()
     assert not twoe._ctx_cache and not any(c.closed for c in held)
+
+
+def test_occupied_subspace_iteration_matches_the_dense_solve():
+    """Chebyshev-filtered subspace iteration (torch on the CPU here) against
+    numpy.linalg.eigh on a Fock-like spectrum: 8 core orbitals near -20.55 Eh, 32
+    valence in [-1.35, -0.45], virtuals in [0.1, 4]; warm-started through a sequence of
+    perturbations of decreasing size, as between SCF iterations."""
+    import torch
+    from mmd.scf import OccupiedSubspace
+    rng = np.random.default_rng(11)
+    N, nocc = 200, 40
+    w = np.concatenate([-20.55 + 0.02 * rng.standard_normal(8), np.sort(rng.uniform(-1.35, -0.45, 32)),
+                        np.sort(rng.uniform(0.1, 4.0, N - 40))])
+    Q, _ = np.linalg.qr(rng.standard_normal((N, N)))
+    F = (Q * w) @ Q.T
+    sub = OccupiedSubspace(nocc, tol=1e-9)
+    assert OccupiedSubspace.applicable(N, nocc)
+    w0, v0 = np.linalg.eigh(F)
+    sub.start(torch.tensor(F), w0, v0)
+    # the core orbitals are split off from the valence slice
+    assert sub.core_count(sub.theta, sub.theta[-1], sub.lmax) == 8
+    for eps in (1e-1, 1e-2, 1e-4, 1e-6):
+        E = rng.standard_normal((N, N))
+        F = F + eps * (E + E.T) / np.linalg.norm(E + E.T, 2)
+        r = sub.solve(torch.tensor(F))
+        assert r is not None
+        theta, V = r[0], r[1].numpy()
+        we, ve = np.linalg.eigh(F)
+        assert np.abs(theta - we[:nocc]).max() < 1e-10
+        Pe = ve[:, :nocc] @ ve[:, :nocc].T
+        assert np.linalg.norm(V @ V.T - Pe) < 1e-7
+    assert sub.fallbacks == 0 and sub.solves == 4
+    # a warm start from an unrelated matrix does not pass the residual test silently
+    G = rng.standard_normal((N, N))
+    r = sub.solve(torch.tensor(G + G.T))
+    if r is not None:
+        wg = np.linalg.eigvalsh(G + G.T)
+        assert np.abs(r[0] - wg[:nocc]).max() < 1e-8
