@@ -1331,95 +1331,120 @@ struct OneEArgs {
   double *S, *T, *V, *M;              // M: 3 blocks of nn
 };
 
+// R^0_tuv (t+u+v <= L, L <= 4) of the nuclear attraction, R[(t*(L+1)+u)*(L+1)+v], from
+// R^(n)_000 = (-2p)^n F_n(p |PC|^2), by the recursion of cython/util.pxi:33-50 level by
+// level (compile-time bounds: the tables live in registers)
 template <int L>
-__device__ void hermite_r_table(const double* boys, double p, double X, double Y, double Z, double* R) {
-  // R[(t*5+u)*5+v] for t+u+v <= L (L <= 4) from R^(n)_000 = (-2p)^n F_n(p |PC|^2)
+__device__ __forceinline__ void hermite_r_table(const double* boys, double p, double X, double Y, double Z,
+                                                double* R) {
+  constexpr int D = L + 1;
   double F[L + 1];
   boys_eval<L>(boys, p * (X * X + Y * Y + Z * Z), F);
-  double cur[5][5][5], nxt[5][5][5];
-  double c = 1.0;
   double R0[L + 1];
+  double c = 1.0;
+#pragma unroll
   for (int n = 0; n <= L; ++n) {
     R0[n] = c * F[n];
     c *= -2.0 * p;
   }
-  // level by level: R^(n) with t+u+v <= L-n
-  for (int t = 0; t < 5; ++t)
-    for (int u = 0; u < 5; ++u)
-      for (int v = 0; v < 5; ++v) cur[t][u][v] = 0.0;
-  cur[0][0][0] = R0[L];
+  double cur[D * D * D];
+  cur[0] = R0[L];
+#pragma unroll
   for (int n = L - 1; n >= 0; --n) {
     const int s = L - n;
+    double nxt[D * D * D];
+#pragma unroll
     for (int t = 0; t <= s; ++t)
+#pragma unroll
       for (int u = 0; u <= s - t; ++u)
+#pragma unroll
         for (int v = 0; v <= s - t - u; ++v) {
           double val;
           if (t + u + v == 0) val = R0[n];
-          else if (t > 0) val = X * cur[t - 1][u][v] + (t > 1 ? (t - 1) * cur[t - 2][u][v] : 0.0);
-          else if (u > 0) val = Y * cur[0][u - 1][v] + (u > 1 ? (u - 1) * cur[0][u - 2][v] : 0.0);
-          else val = Z * cur[0][0][v - 1] + (v > 1 ? (v - 1) * cur[0][0][v - 2] : 0.0);
-          nxt[t][u][v] = val;
+          else if (t > 0) val = X * cur[((t - 1) * D + u) * D + v] + (t > 1 ? (t - 1) * cur[((t - 2) * D + u) * D + v] : 0.0);
+          else if (u > 0) val = Y * cur[(u - 1) * D + v] + (u > 1 ? (u - 1) * cur[(u - 2) * D + v] : 0.0);
+          else val = Z * cur[v - 1] + (v > 1 ? (v - 1) * cur[v - 2] : 0.0);
+          nxt[(t * D + u) * D + v] = val;
         }
+#pragma unroll
     for (int t = 0; t <= s; ++t)
+#pragma unroll
       for (int u = 0; u <= s - t; ++u)
-        for (int v = 0; v <= s - t - u; ++v) cur[t][u][v] = nxt[t][u][v];
+#pragma unroll
+        for (int v = 0; v <= s - t - u; ++v) cur[(t * D + u) * D + v] = nxt[(t * D + u) * D + v];
   }
-  for (int t = 0; t <= L; ++t)
-    for (int u = 0; u <= L - t; ++u)
-      for (int v = 0; v <= L - t - u; ++v) R[(t * 5 + u) * 5 + v] = cur[t][u][v];
+#pragma unroll
+  for (int x = 0; x < D * D * D; ++x) R[x] = cur[x];
 }
 
-// grid: x = shell pair, y = nucleus of the pair's molecule (one thread per (pair,
-// nucleus), so the nuclear-attraction sums run in parallel); the y = 0 thread also
-// writes S, T and the dipole integrals; V is accumulated with atomics
-__global__ void k_one_electron(OneEArgs a) {
-  const int pr = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pr >= a.npair) return;
+// One-electron integrals of the shell pairs of one pair class (la, lb) = (LA, LB),
+// cython/onee.pyx:14-192 as assembled by mmd/molecule.py:235-276.  Grid: x = pair of
+// the class list, y = nucleus of the pair's molecule (one thread per (pair, nucleus),
+// so the nuclear-attraction sums run in parallel); the y = 0 thread also writes S, T
+// and the dipole integrals; V is accumulated with atomics.  Angular momenta are
+// template parameters, so every loop bound is a constant and the tables sit in
+// registers (a runtime-L version kept them in local memory: 13 ms for (H2O)16
+// 6-31G**).
+template <int LA, int LB>
+__global__ void __launch_bounds__(64) k_one_electron(OneEArgs a, const int* __restrict__ plist, int npair) {
+  constexpr int NA = (LA + 1) * (LA + 2) / 2, NB = (LB + 1) * (LB + 2) / 2, L = LA + LB;
+  constexpr int NJ = LB + 3, NT = LA + LB + 3, D = L + 1;
+  const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x0 >= npair) return;
+  const int pr = plist[x0];
   const int sa = a.pa[pr], sb = a.pb[pr];
-  const int la = a.L[sa], lb = a.L[sb];
   const int m = a.sh_mol[sa];
   const int atom = a.atom_begin[m] + (int)blockIdx.y;
   if (atom >= a.atom_end[m]) return;
   const bool first = blockIdx.y == 0;
   const long long base = a.mol_base[m];
   const int N = a.mol_n[m];
-  const double Ax = a.center[3 * sa], Ay = a.center[3 * sa + 1], Az = a.center[3 * sa + 2];
-  const double Bx = a.center[3 * sb], By = a.center[3 * sb + 1], Bz = a.center[3 * sb + 2];
-  const double A[3] = {Ax, Ay, Az}, B[3] = {Bx, By, Bz};
-  const double AB[3] = {Ax - Bx, Ay - By, Az - Bz};
-  const double AB2 = AB[0] * AB[0] + AB[1] * AB[1] + AB[2] * AB[2];
+  const double A[3] = {a.center[3 * sa], a.center[3 * sa + 1], a.center[3 * sa + 2]};
+  const double B[3] = {a.center[3 * sb], a.center[3 * sb + 1], a.center[3 * sb + 2]};
+  const double AB2 = (A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) + (A[2] - B[2]) * (A[2] - B[2]);
   const double* O = a.origin + 3 * m;
-  const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2;
-  double accS[36], accT[36], accV[36], accM[3][36];
-  for (int x = 0; x < 36; ++x) {
+  const double C[3] = {a.atom_xyz[3 * atom], a.atom_xyz[3 * atom + 1], a.atom_xyz[3 * atom + 2]};
+  double accS[NA * NB], accT[NA * NB], accV[NA * NB], accM[3][NA * NB];
+#pragma unroll
+  for (int x = 0; x < NA * NB; ++x) {
     accS[x] = accT[x] = accV[x] = 0.0;
     accM[0][x] = accM[1][x] = accM[2][x] = 0.0;
   }
   const double PI = 3.141592653589793238462643383279;
-  for (int ka = 0; ka < a.nprim[sa]; ++ka)
-    for (int kb = 0; kb < a.nprim[sb]; ++kb) {
-      const double ea = a.exps[a.poff[sa] + ka], eb = a.exps[a.poff[sb] + kb];
+  const int ka_n = a.nprim[sa], kb_n = a.nprim[sb], oa = a.poff[sa], ob = a.poff[sb];
+  for (int ka = 0; ka < ka_n; ++ka)
+    for (int kb = 0; kb < kb_n; ++kb) {
+      const double ea = a.exps[oa + ka], eb = a.exps[ob + kb];
       const double p = ea + eb, ip = 1.0 / p, mu = ea * eb * ip;
-      const double P[3] = {(ea * Ax + eb * Bx) * ip, (ea * Ay + eb * By) * ip, (ea * Az + eb * Bz) * ip};
-      const double cK = a.coefs[a.poff[sa] + ka] * a.coefs[a.poff[sb] + kb] * exp(-mu * AB2);
-      // 1D E[d][i][j][t], i <= 2, j <= lb + 2 <= 4, t <= i + j <= 6
-      double E[3][3][5][7];
+      const double P[3] = {(ea * A[0] + eb * B[0]) * ip, (ea * A[1] + eb * B[1]) * ip, (ea * A[2] + eb * B[2]) * ip};
+      const double cK = a.coefs[oa + ka] * a.coefs[ob + kb] * exp(-mu * AB2);
+      // 1D E[d][i][j][t], i <= LA, j <= LB + 2 (kinetic), t <= i + j (cython/util.pxi:13-28)
+      double E[3][LA + 1][NJ][NT];
       const double i2p = 0.5 * ip;
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         const double XPA = P[d] - A[d], XPB = P[d] - B[d];
-        for (int i = 0; i < 3; ++i)
-          for (int j = 0; j < 5; ++j)
-            for (int t = 0; t < 7; ++t) E[d][i][j][t] = 0.0;
+#pragma unroll
+        for (int i = 0; i <= LA; ++i)
+#pragma unroll
+          for (int j = 0; j < NJ; ++j)
+#pragma unroll
+            for (int t = 0; t < NT; ++t) E[d][i][j][t] = 0.0;
         E[d][0][0][0] = 1.0;
-        for (int i = 0; i < la; ++i)
+#pragma unroll
+        for (int i = 0; i < LA; ++i)
+#pragma unroll
           for (int t = 0; t <= i + 1; ++t) {
             double v = XPA * E[d][i][0][t];
             if (t > 0) v += i2p * E[d][i][0][t - 1];
             if (t + 1 <= i) v += (t + 1) * E[d][i][0][t + 1];
             E[d][i + 1][0][t] = v;
           }
-        for (int j = 0; j < lb + 2; ++j)
-          for (int i = 0; i <= la; ++i)
+#pragma unroll
+        for (int j = 0; j < NJ - 1; ++j)
+#pragma unroll
+          for (int i = 0; i <= LA; ++i)
+#pragma unroll
             for (int t = 0; t <= i + j + 1; ++t) {
               double v = XPB * E[d][i][j][t];
               if (t > 0) v += i2p * E[d][i][j][t - 1];
@@ -1428,15 +1453,18 @@ __global__ void k_one_electron(OneEArgs a) {
             }
       }
       const double s3 = pow(PI * ip, 1.5) * cK;
-      // overlap, kinetic, dipole (the first nucleus's thread)
-      if (first) {
+      if (first) {  // overlap, kinetic, dipole
         int x = 0;
-        for (int xa = la; xa >= 0; --xa)
-          for (int ya = la - xa; ya >= 0; --ya) {
-            const int za = la - xa - ya;
-            for (int xb = lb; xb >= 0; --xb)
-              for (int yb = lb - xb; yb >= 0; --yb, ++x) {
-                const int zb = lb - xb - yb;
+#pragma unroll
+        for (int xa = LA; xa >= 0; --xa)
+#pragma unroll
+          for (int ya = LA - xa; ya >= 0; --ya) {
+            const int za = LA - xa - ya;
+#pragma unroll
+            for (int xb = LB; xb >= 0; --xb)
+#pragma unroll
+              for (int yb = LB - xb; yb >= 0; --yb, ++x) {
+                const int zb = LB - xb - yb;
                 const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
                                    comp_norm(zb);
                 const double Sx = E[0][xa][xb][0], Sy = E[1][ya][yb][0], Sz = E[2][za][zb][0];
@@ -1444,6 +1472,7 @@ __global__ void k_one_electron(OneEArgs a) {
                 const int lbv[3] = {xb, yb, zb};
                 const int lav[3] = {xa, ya, za};
                 double Td[3];
+#pragma unroll
                 for (int d = 0; d < 3; ++d) {
                   const int l2 = lbv[d], l1 = lav[d];
                   double t = (2 * l2 + 1) * eb * E[d][l1][l2][0] - 2.0 * eb * eb * E[d][l1][l2 + 2][0];
@@ -1461,43 +1490,41 @@ __global__ void k_one_electron(OneEArgs a) {
           }
       }
       // nuclear attraction of this thread's nucleus
-      const int L = la + lb;
-      for (int at = atom; at <= atom; ++at) {
-        const double C[3] = {a.atom_xyz[3 * at], a.atom_xyz[3 * at + 1], a.atom_xyz[3 * at + 2]};
-        double R[125];
-        const double X = P[0] - C[0], Y = P[1] - C[1], Z = P[2] - C[2];
-        switch (L) {
-          case 0: hermite_r_table<0>(a.boys, p, X, Y, Z, R); break;
-          case 1: hermite_r_table<1>(a.boys, p, X, Y, Z, R); break;
-          case 2: hermite_r_table<2>(a.boys, p, X, Y, Z, R); break;
-          case 3: hermite_r_table<3>(a.boys, p, X, Y, Z, R); break;
-          default: hermite_r_table<4>(a.boys, p, X, Y, Z, R); break;
+      double R[D * D * D];
+      hermite_r_table<L>(a.boys, p, P[0] - C[0], P[1] - C[1], P[2] - C[2], R);
+      const double pre = -a.atom_Z[atom] * 2.0 * PI * ip * cK;
+      int y = 0;
+#pragma unroll
+      for (int xa = LA; xa >= 0; --xa)
+#pragma unroll
+        for (int ya = LA - xa; ya >= 0; --ya) {
+          const int za = LA - xa - ya;
+#pragma unroll
+          for (int xb = LB; xb >= 0; --xb)
+#pragma unroll
+            for (int yb = LB - xb; yb >= 0; --yb, ++y) {
+              const int zb = LB - xb - yb;
+              const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
+                                 comp_norm(zb);
+              double v = 0.0;
+#pragma unroll
+              for (int t = 0; t <= xa + xb; ++t)
+#pragma unroll
+                for (int u = 0; u <= ya + yb; ++u)
+#pragma unroll
+                  for (int w = 0; w <= za + zb; ++w)
+                    v += E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][w] * R[(t * D + u) * D + w];
+              accV[y] += pre * nab * v;
+            }
         }
-        const double pre = -a.atom_Z[at] * 2.0 * PI * ip * cK;
-        int y = 0;
-        for (int xa = la; xa >= 0; --xa)
-          for (int ya = la - xa; ya >= 0; --ya) {
-            const int za = la - xa - ya;
-            for (int xb = lb; xb >= 0; --xb)
-              for (int yb = lb - xb; yb >= 0; --yb, ++y) {
-                const int zb = lb - xb - yb;
-                const double nab = comp_norm(xa) * comp_norm(ya) * comp_norm(za) * comp_norm(xb) * comp_norm(yb) *
-                                   comp_norm(zb);
-                double v = 0.0;
-                for (int t = 0; t <= xa + xb; ++t)
-                  for (int u = 0; u <= ya + yb; ++u)
-                    for (int w = 0; w <= za + zb; ++w)
-                      v += E[0][xa][xb][t] * E[1][ya][yb][u] * E[2][za][zb][w] * R[(t * 5 + u) * 5 + w];
-                accV[y] += pre * nab * v;
-              }
-          }
-      }
     }
   // scatter (each function pair belongs to exactly one shell pair); V adds this
   // nucleus's share to the zeroed matrix
   int x = 0;
-  for (int ca = 0; ca < na; ++ca)
-    for (int cb = 0; cb < nb; ++cb, ++x) {
+#pragma unroll
+  for (int ca = 0; ca < NA; ++ca)
+#pragma unroll
+    for (int cb = 0; cb < NB; ++cb, ++x) {
       const int i = a.func[sa * kMaxComp + ca], j = a.func[sb * kMaxComp + cb];
       if (i < 0 || j < 0) continue;
       if (sa == sb && cb > ca) continue;  // (ca, cb) already wrote both V[i][j] and V[j][i]
@@ -1509,6 +1536,7 @@ __global__ void k_one_electron(OneEArgs a) {
       a.S[ji] = accS[x];
       a.T[ij] = accT[x];
       a.T[ji] = accT[x];
+#pragma unroll
       for (int d = 0; d < 3; ++d) {
         a.M[d * a.nn + ij] = accM[d][x];
         a.M[d * a.nn + ji] = accM[d][x];
@@ -1573,8 +1601,24 @@ extern "C" int mmdg_one_electron(mmdg_context* h, int natom, const int* atom_mol
   a.M = M;
   int max_atoms = 1;
   for (int m = 0; m < h->nmol; ++m) max_atoms = std::max(max_atoms, ae[m] - ab[m]);
-  k_one_electron<<<dim3((h->npair + 63) / 64, max_atoms), 64, 0, st>>>(a);
-  CUDA_TRY(cudaGetLastError());
+  // one launch per pair class (pairs are stored with la >= lb)
+  static_assert(MMDG_LMAX == 2, "the one-electron dispatch covers l <= 2");
+  for (int la = 0; la <= MMDG_LMAX; ++la)
+    for (int lb = 0; lb <= la; ++lb) {
+      const int c = pair_class(la, lb), n = h->cls_count[c];
+      if (n == 0) continue;
+      const dim3 grid((n + 63) / 64, max_atoms);
+      const int* pl = h->d_cls[c].p;
+      switch (c) {
+        case 0: k_one_electron<0, 0><<<grid, 64, 0, st>>>(a, pl, n); break;
+        case 1: k_one_electron<1, 0><<<grid, 64, 0, st>>>(a, pl, n); break;
+        case 2: k_one_electron<1, 1><<<grid, 64, 0, st>>>(a, pl, n); break;
+        case 3: k_one_electron<2, 0><<<grid, 64, 0, st>>>(a, pl, n); break;
+        case 4: k_one_electron<2, 1><<<grid, 64, 0, st>>>(a, pl, n); break;
+        default: k_one_electron<2, 2><<<grid, 64, 0, st>>>(a, pl, n); break;
+      }
+      CUDA_TRY(cudaGetLastError());
+    }
   CUDA_TRY(cudaStreamSynchronize(st));  // the temporary atom buffers are freed on return
   return MMDG_OK;
 }

@@ -267,18 +267,27 @@ class Molecule(SCF, Forces):
         self.V = self._dev["V"].cpu().numpy()
         self.M = self._dev["M"].cpu().numpy()
         self.mu = np.zeros(3, dtype="complex")
+        # nuclear repulsion over the atom pairs in itertools.combinations order, summed
+        # sequentially (np.add.accumulate) like the reference's loop
         self.nuc_energy = 0.0
-        for pair in itertools.combinations(self.atoms, 2):
-            self.nuc_energy += pair[0].charge * pair[1].charge / np.linalg.norm(pair[0].origin - pair[1].origin)
+        if nat > 1:
+            i, j = np.triu_indices(nat, 1)
+            R = xyz.reshape(-1, 3)
+            d = R[i] - R[j]
+            terms = Zs[i] * Zs[j] / np.sqrt(np.einsum("ij,ij->i", d, d))
+            self.nuc_energy = float(np.add.accumulate(terms)[-1])
         self.Core = self.T + self.V
         # S^{-1/2} and S^{1/2} by the symmetric eigendecomposition of S on the host cores
-        # (LAPACK dsyevd, the SCF's own eigensolver up to ~1000 functions): one solve per
-        # basis, and no dependence on torch's CUDA linear-algebra library
+        # (LAPACK dsyevd, the SCF's own eigensolver up to ~1000 functions: no dependence
+        # on torch's CUDA linear-algebra library); the two products on the GPU
         from .scf import host_eigh
         w, U = host_eigh(self.S)
-        self.X = (U * (1.0 / np.sqrt(w))) @ U.T
-        self.U = (U * np.sqrt(w)) @ U.T
-        self._dev["X"] = torch.as_tensor(self.X, device=dev)
+        Ud = torch.as_tensor(U, device=dev)
+        wd = torch.as_tensor(w, device=dev)
+        Xd = (Ud * (1.0 / torch.sqrt(wd))) @ Ud.T
+        self._dev["X"] = Xd
+        self.X = Xd.cpu().numpy()
+        self.U = ((Ud * torch.sqrt(wd)) @ Ud.T).cpu().numpy()
         self._dev["Core"] = self._dev["T"] + self._dev["V"]
 
     def two_electron_integrals(self):

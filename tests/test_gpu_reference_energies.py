@@ -51,8 +51,8 @@ def test_combined_form_matches_the_reference_energies():
 
 def test_chosen_single_molecule_form_matches_the_reference_energies():
     """The single-molecule chosen form of the benchmark -- learned guess, FP32 below
-    Schwarz 1e-3, stop at ||dP|| < 1e-5, occupied orbitals by subspace iteration, polish
-    build (FP32 below 1e-7) -- against the reference's energies, and the same run with
+    Schwarz 1e-1, stop at ||dP|| < 1e-5, occupied orbitals by subspace iteration, polish
+    build (FP32 below 1e-5) -- against the reference's energies, and the same run with
     the dense eigensolver within 1e-9 Eh of it."""
     from mmd import guess as G
     from mmd.clusters import water_cluster
@@ -64,8 +64,8 @@ def test_chosen_single_molecule_form_matches_the_reference_energies():
         for eig in ("subspace", "dense"):
             mol = Molecule(g, "6-31g")
             P0 = G.predict_density(net, mol)
-            out[eig] = float(mol.RHF(doPrint=False, direct=True, fp32_below=1e-3, guess=P0, conver=1e-5, polish=True,
-                                     polish_fp32_below=1e-7, eigensolver=eig))
+            out[eig] = float(mol.RHF(doPrint=False, direct=True, fp32_below=1e-1, guess=P0, conver=1e-5, polish=True,
+                                     polish_fp32_below=1e-5, eigensolver=eig))
             assert mol.is_converged
             if eig == "subspace":
                 assert mol.subspace is not None and mol.subspace.solves > 0
