@@ -51,12 +51,13 @@ WORKLOAD = {"workload": "(H2O)16 6-31G** direct RHF", "n_water": 16, "lattice": 
 # the same rule and prints its own figure as config.fq_per_build).  Used by the
 # reference arm, which cannot run the 400-function SCF itself.
 FQ_PER_BUILD = 198282802.0
-# DRAM bytes (read + write) of one launch of the top class kernels in the first, full
-# Fock build of this workload, from one ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum; summary and command in profiles/k_fock_fp64_pipe_h2o16.md).
-DRAM_BYTES_PER_LAUNCH = {"1000": 47.3e6, "0000": 23.9e6, "1010": 25.0e6, "1110": 15.6e6, "2111": 4.9e6}
+# DRAM bytes (read + write) per launch of the dominant class kernel on this workload,
+# mean of launches 5-7 of k_fock<MD_1000> (early Fock builds of the warm-up SCF) in one
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; summary and command in
+# profiles/k_fock_1000_h2o16.md).
+DRAM_BYTES_PER_LAUNCH = {"1000": 49.11e6}
 # FP64-pipe busy fraction of the same launches (sm__pipe_fp64_cycles_active, same capture)
-FP64_PIPE_BUSY = {"1000": 0.733, "0000": 0.545, "1010": 0.694, "1110": 0.573, "2111": 0.714}
+FP64_PIPE_BUSY = {"1000": 0.710}
 
 
 def _env():
@@ -536,10 +537,13 @@ def consumers_bench():
 CHOSEN_FP32_BELOW = 1e-1
 CHOSEN_CONVER = 1e-5
 CHOSEN_POLISH_FP32_BELOW = 1e-5
-# Between iterations the chosen form solves for the occupied orbitals only, by
-# Chebyshev-filtered subspace iteration on the GPU (mmd.scf.OccupiedSubspace, residuals
-# below conver / 1000) instead of the dense host eigensolve of all N orbitals.
-CHOSEN_EIGENSOLVER = "subspace"
+# Eigensolver of the chosen form's iterations: the dense host solve of all N orbitals.
+# The occupied-subspace solver (mmd.scf.OccupiedSubspace: Chebyshev-filtered subspace
+# iteration on the GPU, 1.7 passes per iteration) measured slower at N = 400 (0.376
+# against 0.359 s to converge): its ~25 small GEMMs and two host round trips per pass
+# cost about what LAPACK's dsyevd takes for 400 x 400 (7 ms).  The line keeps it as an
+# ablation.
+CHOSEN_EIGENSOLVER = "dense"
 
 
 def chosen_form_ttc(geom, ttc_plain, iters_plain, plain_mol, thr=CHOSEN_FP32_BELOW, conver=CHOSEN_CONVER,
@@ -744,8 +748,8 @@ def gpu_arm(args):
                     "energy_diff_vs_plain_fp64_gpu_polished")
             a = chosen_form_ttc(geom, ttc, iters, m2, conver=1e-8, polish_fp32_below=0.0)
             chosen["at_reference_stopping_rule"] = {k: a[k] for k in keep}
-            a = chosen_form_ttc(geom, ttc, iters, m2, eigensolver="dense")
-            chosen["with_dense_eigensolver"] = {k: a[k] for k in keep}
+            a = chosen_form_ttc(geom, ttc, iters, m2, eigensolver="subspace")
+            chosen["with_subspace_eigensolver"] = {k: a[k] for k in keep + ("subspace",)}
             b = chosen_form_ttc(geom, ttc, iters, m2, thr=0.0, polish_fp32_below=0.0, learned=False,
                                 eigensolver="dense")
             chosen["plain_fp64_at_chosen_stopping_rule"] = {k: b[k] for k in keep}
