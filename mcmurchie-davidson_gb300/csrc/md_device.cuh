@@ -227,6 +227,18 @@ struct Ctx<double> {
   __device__ __forceinline__ void hermite_r0(int i, int j, double* Rn, double& X, double& Y, double& Z) const {
     hermite_r0_pp<L>(g->pP[i], g->pP[j], Rn, X, Y, Z);
   }
+  // R^(n)_000 = (p+q)^{-1/2} (-2 alpha)^n F_n(T), n = 0..L, T = alpha |PQ|^2, alpha =
+  // pq/(p+q), and PQ = (X, Y, Z).  For L <= 4 the branch is taken before any FP64
+  // work that only one side needs, on an FP32 estimate of T (FP32 and integer pipes):
+  //   near (T < 48 - 1/32): 1/sqrt(p+q), alpha, T, the tabulated Boys function;
+  //   far: the asymptotic F_n = (2n-1)!! sqrt(pi) / (2^{n+1} T^{n+1/2}) (the e^{-T}
+  //   terms are below 5e-15 relative for n <= 4) turns R^(n) into the point-charge
+  //   form R^(0) = sqrt(pi)/2 / (sqrt(pq) |PQ|), R^(n) = -(2n-1) R^(n-1) / |PQ|^2,
+  //   which needs 1/sqrt(pq |PQ|^2) and no Boys function or alpha at all.
+  // Both sides take their one reciprocal square root from the same rsqrt_dd call
+  // (argument p+q or pq |PQ|^2), so a warp whose lanes straddle T = 48 issues it once.
+  // A near lane whose FP64 T lands past the table still gets the asymptotic form
+  // inside boys_eval (its own test), so the table is never read out of range.
   template <int L>
   __device__ __forceinline__ void hermite_r0_pp(const PP& a, const PP& b, double* Rn, double& X, double& Y,
                                                 double& Z) const {
@@ -234,6 +246,35 @@ struct Ctx<double> {
     Y = a.z - b.z;
     Z = a.w - b.w;
     const double r2 = fma(X, X, fma(Y, Y, Z * Z));
+    if constexpr (L <= 4) {
+      const double pq = a.x * b.x, s = a.x + b.x, pqr2 = pq * r2;
+      const float Tf = __fdividef(f32_of_nonneg(pqr2), f32_of_nonneg(s));
+      const bool far = Tf >= float(kBoysTaylorMax);
+      const double rr = rsqrt_dd(far ? pqr2 : s);
+      if (far) {
+        ++nasym;
+        Rn[0] = kHalfSqrtPi * rr;
+        if (L > 0) {
+          const double nir2 = (rr * rr) * -pq;  // -1/|PQ|^2
+          Rn[1] = Rn[0] * nir2;
+#pragma unroll
+          for (int n = 2; n <= L; ++n) Rn[n] = Rn[n - 1] * (double(2 * n - 1) * nir2);
+        }
+      } else {
+        const double alpha = pq * (rr * rr);
+        const double T = alpha * r2;
+        double F[L + 1];
+        boys_eval<L>(g->boys64, T, F);
+        double c = rr;  // 2 pi^{5/2} is folded into the E' coefficients
+        const double m2a = -2.0 * alpha;
+#pragma unroll
+        for (int n = 0; n <= L; ++n) {
+          Rn[n] = c * F[n];
+          c *= m2a;
+        }
+      }
+      return;
+    }
     const double rsum = rsqrt_dd(a.x + b.x);
     const double alpha = a.x * b.x * (rsum * rsum);
     double F[L + 1];
