@@ -193,6 +193,15 @@ def cpu_sample(spec_path, cores, steps, warmup):
     out = {"kind": spec["kind"], "cores": cores, "t_skip_s": ts, "t_full_s": tf, "t_candidate_s": t_cand,
            "t_eri_s": t_eri, "t_build_1core_s": t_build, "builds_per_s": cores / t_build,
            "quartets_per_s_1core": 1.0 / t_eri, "steps": steps}
+    anchor = spec.get("anchor")
+    if anchor:
+        # one whole formPT call of (H2O)2 on one core against the extrapolation's
+        # prediction for it (the same per-candidate and per-survivor costs)
+        with ctx.Pool(1, initializer=_ref_worker_init, initargs=(anchor["spec_path"],)) as pool:
+            t_anchor = pool.map(_ref_worker_run, ["full"])[0]
+        pred = anchor["n_cand"] * t_cand + anchor["n_surv"] * t_eri
+        out["anchor"] = {"workload": anchor["workload"], "candidates": anchor["n_cand"], "survivors": anchor["n_surv"],
+                         "measured_s": t_anchor, "predicted_s": pred, "measured_over_predicted": t_anchor / pred}
     print(json.dumps(out))
 
 
@@ -214,20 +223,48 @@ def _monomer_spec(kind):
     N = len(bfs)
     P1 = g["formPT0_P"]
     scr = g["screen"]
-    # survivors of the reference's screening rule for dP = P1 (fock.pyx:46-57)
+    n_cand, n_surv = _formpt_counts(P1, scr)
+    return {"kind": kind, "bfs": bfs, "screen": scr.tolist(), "P": P1.tolist(),
+            "n_cand_monomer": n_cand, "n_surv_monomer": n_surv}
+
+
+def _formpt_counts(P, scr, tol=1e-12):
+    """Candidate and surviving function quartets of one formPT call with dP = P: the
+    reference's screening rule (fock.pyx:46-57) over its canonical quartets."""
+    import numpy as np
+    N = P.shape[0]
     sq = np.sqrt(scr)
     iu = np.array([(i, j) for i in range(N) for j in range(i + 1)])
-    d = np.abs(P1)
+    d = np.abs(P)
     n_surv = 0
     for a in range(len(iu)):
         i, j = iu[a]
         kl = iu[: a + 1]
         k, l = kl[:, 0], kl[:, 1]
         dm = np.maximum.reduce([np.full(len(kl), 4 * d[i, j]), 4 * d[k, l], d[i, k], d[i, l], d[j, k], d[j, l]])
-        n_surv += int(np.sum(sq[a] * sq[: a + 1] * dm >= 1e-12))
+        n_surv += int(np.sum(sq[a] * sq[: a + 1] * dm >= tol))
     npair = N * (N + 1) // 2
-    return {"kind": kind, "bfs": bfs, "screen": scr.tolist(), "P": P1.tolist(),
-            "n_cand_monomer": npair * (npair + 1) // 2, "n_surv_monomer": n_surv}
+    return npair * (npair + 1) // 2, n_surv
+
+
+def _anchor_spec(kind):
+    """The (H2O)2 / 6-31G** formPT call of tests/golden/h2o2_631gss_formpt.npz (the
+    first call of the reference's own direct RHF) in the worker's format."""
+    import numpy as np
+    sys.path.insert(0, PKG)
+    from mmd.molecule import Molecule
+    g = np.load(os.path.join(REPO, "tests", "golden", "h2o2_631gss_formpt.npz"))
+    m = Molecule(str(g["geometry"]), "6-31gss")
+    bfs = []
+    for atom in m.atoms:
+        for momentum, prims in m.basis_data[atom.charge]:
+            ex = [e for e, c in prims]
+            co = [c for e, c in prims]
+            for sh in m.momentum2shell(momentum):
+                bfs.append((list(map(float, atom.origin)), list(sh), ex, co))
+    n_cand, n_surv = _formpt_counts(g["P"], g["screen"])
+    return {"kind": kind, "bfs": bfs, "screen": g["screen"].tolist(), "P": g["P"].tolist(),
+            "n_cand": n_cand, "n_surv": n_surv, "workload": f"(H2O)2 6-31G** (N={len(bfs)}), one formPT call, one core"}
 
 
 def run_cpu_sample(n_cand_target, n_surv_target, steps, warmup, cores=None):
@@ -240,6 +277,12 @@ def run_cpu_sample(n_cand_target, n_surv_target, steps, warmup, cores=None):
     spec["n_cand_target"] = n_cand_target
     spec["n_surv_target"] = n_surv_target
     cores = cores or os.cpu_count()
+    aspec = _anchor_spec(kind)
+    with tempfile.NamedTemporaryFile("w", suffix=".json", delete=False) as f:
+        json.dump(aspec, f)
+        apath = f.name
+    spec["anchor"] = {"spec_path": apath, "n_cand": aspec["n_cand"], "n_surv": aspec["n_surv"],
+                      "workload": aspec["workload"]}
     with tempfile.NamedTemporaryFile("w", suffix=".json", delete=False) as f:
         json.dump(spec, f)
         path = f.name
@@ -249,6 +292,7 @@ def run_cpu_sample(n_cand_target, n_surv_target, steps, warmup, cores=None):
                              capture_output=True, text=True, check=True, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
     finally:
         os.unlink(path)
+        os.unlink(apath)
     res = json.loads(out.stdout.strip().splitlines()[-1])
     res["sample"] = (f"reference formPT on water/6-31G** (N=25, {spec['n_cand_monomer']} candidate and "
                      f"{spec['n_surv_monomer']} surviving quartets) in {cores} processes, dP=0 and dP=P1 per step; "

@@ -129,6 +129,22 @@ def test_full_eri_tensor_and_formPT_of_water_clusters_vs_oracle(n):
         assert gerr < 1e-12, (n, gerr)
 
 
+def test_formPT_of_h2o2_matches_the_reference_call():
+    """The first formPT call of the reference's own direct RHF on the benchmark
+    generator's (H2O)2 / 6-31G** (inputs, output and its Schwarz table recorded by
+    tests/golden/make_golden_h2o2_formpt.py): the GPU formPT through the reference's
+    signature gives the reference's G to 1e-12."""
+    from mmd.integrals.fock import formPT
+    from mmd.molecule import Molecule
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "h2o2_631gss_formpt.npz"))
+    mol = Molecule(str(g["geometry"]), "6-31gss")
+    N = mol.nbasis
+    screen = {x: float(v) for x, v in enumerate(g["screen"])}
+    G = formPT(g["P"].astype(complex), np.zeros((N, N), dtype=complex), mol.bfs, N, screen, float(g["tol"]))
+    assert np.abs(G.real - g["G"]).max() < 1e-12
+    assert np.abs(mol.context.screen() - g["screen"]).max() < 1e-12
+
+
 def test_h2o16_stratified_shell_quartets_vs_oracle():
     import oracle as O
     from mmd.integrals.shells import shells_from_bfs

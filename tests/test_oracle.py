@@ -212,3 +212,26 @@ def test_partial_formPT_adds_up_to_formPT(golden):
                  for r in range(world)]
         assert all(np.abs(p).max() > 0 for p in parts)
         assert np.max(np.abs(sum(parts) - ref)) < 1e-13
+
+
+def test_oracle_formPT_matches_the_reference_call_on_h2o2():
+    """The oracle's formPT against the reference's own first formPT call of its direct
+    RHF on (H2O)2 / 6-31G** (813,450 candidate quartets; fixture made by
+    tests/golden/make_golden_h2o2_formpt.py), run over ij ranges in processes."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                    "mcmurchie-davidson_gb300"))
+    from mmd.molecule import Molecule
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "h2o2_631gss_formpt.npz"))
+    mol = Molecule(str(g["geometry"]), "6-31gss")
+    bfs = []
+    for atom in mol.atoms:
+        for momentum, prims in mol.basis_data[atom.charge]:
+            ex = [e for e, c in prims]
+            co = [c for e, c in prims]
+            for shell in mol.momentum2shell(momentum):
+                bfs.append(O.Basis(atom.origin, shell, len(ex), ex, co))
+    N = len(bfs)
+    assert np.abs(O.screen_table(bfs) - g["screen"]).max() < 1e-13
+    G = O.parallel_formPT(g["P"], np.zeros((N, N)), bfs, N, g["screen"], float(g["tol"]))
+    assert np.abs(G - g["G"]).max() < 1e-12
