@@ -261,6 +261,7 @@ struct mmdg_context {
   int total_keys = 0;
   DevBuf<long long> d_keyoff;
   DevBuf<unsigned> d_qn;  // [2*total_keys]: FP64 and FP32 bucket lengths
+  DevBuf<unsigned long long> d_work;  // [2*MMDG_NCLASS]: work counters of the FP64 and FP32 class launches
   Geometry geom() const {
     Geometry g;
     g.pP = d_pP.p;
@@ -850,7 +851,7 @@ extern "C" int mmdg_device_bytes(mmdg_context* h, long long* bytes) {
   MMDG_ADD(d_pa); MMDG_ADD(d_pb); MMDG_ADD(d_prb); MMDG_ADD(d_prc); MMDG_ADD(d_eoff);
   MMDG_ADD(d_pP); MMDG_ADD(d_pPf); MMDG_ADD(d_E64); MMDG_ADD(d_E32); MMDG_ADD(d_Q);
   MMDG_ADD(d_mol_shell0); MMDG_ADD(d_screen); MMDG_ADD(d_sq); MMDG_ADD(d_sqf); MMDG_ADD(d_dPf); MMDG_ADD(d_Dsh);
-  MMDG_ADD(d_counters); MMDG_ADD(d_q64); MMDG_ADD(d_q32); MMDG_ADD(d_keyoff); MMDG_ADD(d_qn);
+  MMDG_ADD(d_counters); MMDG_ADD(d_q64); MMDG_ADD(d_q32); MMDG_ADD(d_keyoff); MMDG_ADD(d_qn); MMDG_ADD(d_work);
   MMDG_ADD(d_pair_owner); MMDG_ADD(d_pair_canon);
   for (int c = 0; c < kNumPairClasses; ++c) {
     MMDG_ADD(d_cls[c]); MMDG_ADD(d_cls_moff[c]); MMDG_ADD(d_gslot[c]);
@@ -1049,6 +1050,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
   f.tolf_lo = float(tol * (1.0 - 1e-4));
   f.tolf_hi = float(tol * (1.0 + 1e-4));
   f.counters = nullptr;
+  f.work = nullptr;  // set per launch below
   f.pair_owner = h->nparts > 1 ? h->d_pair_owner.p : nullptr;
   f.pair_canon = h->d_pair_canon.p;
   f.part = h->part;
@@ -1080,6 +1082,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
     h->q_total = tot;
     h->total_keys = nk;
     if (h->d_q64.alloc(tot > 0 ? tot : 1) != cudaSuccess || h->d_qn.alloc(2 * (nk > 0 ? nk : 1)) != cudaSuccess ||
+        h->d_work.alloc(2 * MMDG_NCLASS) != cudaSuccess ||
         h->d_keyoff.upload(koff.empty() ? std::vector<long long>{0} : koff) != cudaSuccess) {
       h->q_off.clear();
       return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the quartet lists");
@@ -1090,6 +1093,7 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
       return fail(MMDG_E_NOMEM, "mmdg_fock: cannot allocate the FP32 quartet lists");
   }
   CUDA_TRY(cudaMemsetAsync(h->d_qn.p, 0, sizeof(unsigned) * 2 * (h->total_keys > 0 ? h->total_keys : 1), st));
+  CUDA_TRY(cudaMemsetAsync(h->d_work.p, 0, sizeof(unsigned long long) * 2 * MMDG_NCLASS, st));
   cudaEvent_t ev[2 * MMDG_NCLASS];
   if (class_ms)
     for (int k = 0; k < 2 * MMDG_NCLASS; ++k) CUDA_TRY(cudaEventCreate(&ev[k]));
@@ -1131,11 +1135,14 @@ static int fock_impl(mmdg_context* h, const double* dP, double* G, double tol, d
                      h->d_cls_moff[ck].p};
       const long long* ko = h->d_keyoff.p + h->kbase[ci];
       const int grid = h->class_grid[ci], blk = h->class_block[ci], item = h->class_item[ci];
+      f.work = h->d_work.p + 2 * ci;
       CUDA_TRY(e.fock(0, g, f, cl, h->d_q64.p + h->q_off[ci], h->d_qn.p + h->kbase[ci], ko, h->nkeys[ci], grid, blk,
                       item, cs));
-      if (split > 0.f)
+      if (split > 0.f) {
+        f.work = h->d_work.p + 2 * ci + 1;
         CUDA_TRY(e.fock(1, g, f, cl, h->d_q32.p + h->q_off[ci], h->d_qn.p + h->total_keys + h->kbase[ci], ko,
                         h->nkeys[ci], grid, blk, item, cs));
+      }
     }
     if (class_ms) CUDA_TRY(cudaEventRecord(ev[2 * ci + 1], st));
     ++ci;

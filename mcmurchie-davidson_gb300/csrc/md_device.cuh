@@ -389,6 +389,9 @@ struct FockArgs {
   const int* pair_owner;  // per shell pair
   const int* pair_canon;  // canonical index s1(s1+1)/2 + s2 of every shell pair (per molecule)
   int part;
+  // per launch: the next unclaimed work item of the launch's list (zeroed before every
+  // build); warps claim items from it, so the SMs that draw cheap quartets draw more
+  unsigned long long* work;
 };
 
 template <int NB, int ND>

@@ -127,9 +127,21 @@ static __global__ void __launch_bounds__(kThreads) k_screen(Geometry g, FockArgs
 
 constexpr int kMaxKeys = 256;
 
-// Evaluation of a bucketed quartet list: persistent grid-stride loop over
-// (chunk, bucket, quartet), chunk-major, so that a warp shares its chunk (code
-// path) and, inside a bucket, its primitive trip counts; heaviest buckets first.
+// Evaluation of a bucketed quartet list: persistent loop over (chunk, bucket,
+// quartet), chunk-major, so that a warp shares its chunk (code path) and, inside a
+// bucket, its primitive trip counts; heaviest buckets first.
+//
+// FP64 lists of at least 8 items per thread claim their work dynamically: each warp
+// takes the next 32 items from the launch's counter (one atomic per claim, issued one
+// claim ahead so its round trip overlaps the work), lane l the item base + l.  With
+// the static grid-stride split the average SM sat idle for 20 % of a (ps|ss) launch
+// while the slowest finished (ncu: sm__cycles_active avg 9.9M, max 12.4M cycles of
+// 12.4M); claiming cut the (H2O)16 class kernels run one after another from 44.8 to
+// 40.0 ms (same GPU, two repeats each).  Claims of 128 or 256 items were 1.8-2.7x
+// slower (the warps' working set of pairs and E' rows spreads over that many more
+// quartets); short lists (a few items per thread: the near quartets of a mixed
+// build) and the memory-latency-bound FP32 lists ran 5-35 % slower with claims, so
+// they keep the static split.
 template <class MD, typename Real>
 __global__ void __launch_bounds__(kMaxFockBlock) k_fock(Geometry g, FockArgs f, ClassLaunch cl, const int2* list,
                                                    const unsigned* count, const long long* key_off, int nkeys) {
@@ -151,30 +163,52 @@ __global__ void __launch_bounds__(kMaxFockBlock) k_fock(Geometry g, FockArgs f, 
   Real* rs = reinterpret_cast<Real*>(smem_d) + threadIdx.x;
   unsigned nfq = 0, nsq = 0, npq = 0, nbp = 0, nas = 0;
   int key = 0;
-  // block size: kThreads for classes with shared-memory R tables, else 64..256 (tile)
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int chunk = (int)(idx / n);
-    // buckets run from the heaviest (most primitive pairs, stored last) to the
-    // lightest, so the persistent loop's last round holds the cheapest quartets
-    const unsigned r = n - 1u - (unsigned)(idx - (long long)chunk * n);
-    if (r < s_pre[key]) key = 0;
-    while (r >= s_pre[key + 1]) ++key;
-    const int2 e = list[s_off[key] + (r - s_pre[key])];
-    const int bp = __ldg(cl.bra + e.x), kp = __ldg(cl.ket + e.y);
-    const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
-    Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, rs);
-    c.chunk = MD::NCHUNK > 1 ? chunk : -1;
-    QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, __ldg(g.sh_mol + sa)};
-    FockDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, f, q);
-    MD::run(c, dg);
-    nfq += dg.nfq;
-    if (chunk == 0) {
-      ++nsq;
-      npq += unsigned((c.bra_end - c.bra_begin) * (c.ket_end - c.ket_begin));
-      nbp += unsigned(c.bra_end - c.bra_begin);
-      nas += c.nasym;
+  // block size: kThreads for classes with shared-memory R tables, else 64..256 (tile),
+  // a multiple of 32 either way, so every warp is full
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const bool kDynamic = sizeof(Real) == 8 && total >= 8 * nthreads;
+  const unsigned lane = threadIdx.x & 31u;
+  unsigned long long base = 0, next = 0;
+  long long sidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (kDynamic) {
+    if (lane == 0) base = atomicAdd(f.work, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+  }
+  for (;;) {
+    long long idx;
+    if (kDynamic) {
+      if (base >= (unsigned long long)total) break;  // warp-uniform
+      if (lane == 0) next = atomicAdd(f.work, 32ull);  // the next claim, in flight during this one
+      idx = (long long)base + lane;
+    } else {
+      if (sidx >= total) break;
+      idx = sidx;
     }
+    if (idx < total) {
+      const int chunk = (int)(idx / n);
+      // buckets run from the heaviest (most primitive pairs, stored last) to the
+      // lightest, so the loop's last rounds hold the cheapest quartets
+      const unsigned r = n - 1u - (unsigned)(idx - (long long)chunk * n);
+      if (r < s_pre[key]) key = 0;
+      while (r >= s_pre[key + 1]) ++key;
+      const int2 e = list[s_off[key] + (r - s_pre[key])];
+      const int bp = __ldg(cl.bra + e.x), kp = __ldg(cl.ket + e.y);
+      const int sa = __ldg(g.pa + bp), sb = __ldg(g.pb + bp), sc = __ldg(g.pa + kp), sd = __ldg(g.pb + kp);
+      Ctx<Real> c = make_ctx<MD, Real>(g, bp, kp, rs);
+      c.chunk = MD::NCHUNK > 1 ? chunk : -1;
+      QuartetInfo q{sa, sb, sc, sd, sa == sb, sc == sd, bp == kp, __ldg(g.sh_mol + sa)};
+      FockDigest<ncart(MD::LB), ncart(MD::LD)> dg(g, f, q);
+      MD::run(c, dg);
+      nfq += dg.nfq;
+      if (chunk == 0) {
+        ++nsq;
+        npq += unsigned((c.bra_end - c.bra_begin) * (c.ket_end - c.ket_begin));
+        nbp += unsigned(c.bra_end - c.bra_begin);
+        nas += c.nasym;
+      }
+    }
+    if (kDynamic) base = __shfl_sync(0xffffffffu, next, 0);
+    else sidx += nthreads;
   }
   if (f.counters) {
     const unsigned mask = __activemask();
