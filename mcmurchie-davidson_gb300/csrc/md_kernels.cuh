@@ -136,8 +136,9 @@ constexpr int kMaxKeys = 256;
 // claim ahead so its round trip overlaps the work), lane l the item base + l.  With
 // the static grid-stride split the average SM sat idle for 20 % of a (ps|ss) launch
 // while the slowest finished (ncu: sm__cycles_active avg 9.9M, max 12.4M cycles of
-// 12.4M); claiming cut the (H2O)16 class kernels run one after another from 44.8 to
-// 40.0 ms (same GPU, two repeats each).  Claims of 128 or 256 items were 1.8-2.7x
+// 12.4M); with the warp kernel's claims (md_warp.cuh) it cut the (H2O)16 class kernels
+// run one after another from 44.9 to 38.6 ms and the 4-stream build from 36.4 to
+// 34.9 ms (same GPU, two repeats each).  Claims of 128 or 256 items were 1.8-2.7x
 // slower (the warps' working set of pairs and E' rows spreads over that many more
 // quartets); short lists (a few items per thread: the near quartets of a mixed
 // build) and the memory-latency-bound FP32 lists ran 5-35 % slower with claims, so
