@@ -82,8 +82,10 @@ def shells_from_bfs(bfs) -> ShellSet:
         origin = np.asarray(b.origin, dtype=np.float64).reshape(3)
         exps = np.asarray(b.exps, dtype=np.float64)[:k]
         w = np.asarray(b.norm, dtype=np.float64)[:k] * np.asarray(b.coefs, dtype=np.float64)[:k] / comp_norm(lmn)
-        join = (cur is not None and cur[1] == L and c > cur[4] and np.array_equal(cur[0], origin)
-                and np.array_equal(cur[2], exps) and np.allclose(cur[3], w, rtol=1e-12, atol=0.0))
+        # (the weights test is np.allclose(cur_w, w, rtol=1e-12, atol=0) written out)
+        join = (cur is not None and cur[1] == L and c > cur[4] and cur[2].shape == exps.shape
+                and bool((cur[0] == origin).all()) and bool((cur[2] == exps).all())
+                and bool((np.abs(cur[3] - w) <= 1e-12 * np.abs(w)).all()))
         if join:
             fn_[-1][c] = f
             cur = (cur[0], cur[1], cur[2], cur[3], c)

@@ -55,11 +55,11 @@ class Basis:
         f2 = _fact2(2 * l - 1) * _fact2(2 * m - 1) * _fact2(2 * n - 1)
         self.norm = np.sqrt(np.power(2, 2 * L + 1.5) * np.power(self.exps, L + 1.5) / f2 / np.power(np.pi, 1.5))
         prefactor = np.power(np.pi, 1.5) * f2 / np.power(2.0, L)
-        N = 0.0
-        for ia in range(self.num_exps):
-            for ib in range(self.num_exps):
-                N += self.norm[ia] * self.norm[ib] * self.coefs[ia] * self.coefs[ib] / \
-                    np.power(self.exps[ia] + self.exps[ib], L + 1.5)
+        # the double sum over primitive pairs, each term formed in the reference's
+        # operation order and accumulated left to right in its (ia, ib) order
+        nm, c, e = self.norm, self.coefs, self.exps
+        terms = nm[:, None] * nm[None, :] * c[:, None] * c[None, :] / np.power(e[:, None] + e[None, :], L + 1.5)
+        N = 0.0 + np.add.accumulate(terms.ravel())[-1]
         N *= prefactor
         N = np.power(N, -0.5)
         self.coefs *= N
