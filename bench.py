@@ -51,13 +51,14 @@ WORKLOAD = {"workload": "(H2O)16 6-31G** direct RHF", "n_water": 16, "lattice": 
 # the same rule and prints its own figure as config.fq_per_build).  Used by the
 # reference arm, which cannot run the 400-function SCF itself.
 FQ_PER_BUILD = 198282802.0
-# DRAM bytes (read + write) per launch of the dominant class kernel on this workload,
-# mean of launches 5-7 of k_fock<MD_1000> (early Fock builds of the warm-up SCF) in one
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; summary and command in
-# profiles/k_fock_1000_h2o16.md).
-DRAM_BYTES_PER_LAUNCH = {"1000": 49.11e6}
-# FP64-pipe busy fraction of the same launches (sm__pipe_fp64_cycles_active, same capture)
-FP64_PIPE_BUSY = {"1000": 0.710}
+# DRAM bytes (read + write) per launch of the dominant class kernel on this workload:
+# launch 5 of k_fock<MD_1000> (an early Fock build of the warm-up SCF) in one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum; summary and command in
+# profiles/k_fock_1000_full_h2o16.md).
+DRAM_BYTES_PER_LAUNCH = {"1000": 49.99e6}
+# FP64-pipe busy fraction of the same launch over its elapsed cycles
+# (sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_elapsed, same capture)
+FP64_PIPE_BUSY = {"1000": 0.872}
 
 
 def _env():
@@ -807,7 +808,7 @@ def gpu_arm(args):
             cb = run_cpu_sample(npair * (npair + 1) // 2, fq_per_build, steps=2, warmup=1)
             cpu = {"value": cb["builds_per_s"], "unit": "Fock builds/s", "cores": cb["cores"], "kind": cb["kind"],
                    "sample": cb["sample"], "t_build_1core_s": cb["t_build_1core_s"],
-                   "quartets_per_s_1core": cb["quartets_per_s_1core"]}
+                   "quartets_per_s_1core": cb["quartets_per_s_1core"], "anchor": cb.get("anchor")}
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "error": str(e)[:300]}
     # our kernels per Fock build: k_prep_density, k_shell_dmax, one k_screen per class,
@@ -877,7 +878,7 @@ def reference_arm(args):
             "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded cluster geometry)", "config": dict(WORKLOAD),
             "cpu_baseline": {"value": v, "unit": "Fock builds/s", "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"]},
+                             "sample": cb["sample"], "anchor": cb.get("anchor")},
             "e2e": {"value": v, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
