@@ -195,6 +195,7 @@ struct mmdg_context {
   bool have_basis = false;
   DevBuf<double> boys64;
   DevBuf<float> boys32;
+  DevBuf<float> boysdf;  // the FP64 rows as (hi, lo) float pairs
   // basis
   int nmol = 0, nshell = 0;
   std::vector<int> mol_n, mol_ns;
@@ -284,6 +285,7 @@ struct mmdg_context {
     g.mol_tbase = d_mol_tbase.p;
     g.boys64 = boys64.p;
     g.boys32 = boys32.p;
+    g.boysdf = boysdf.p;
     return g;
   }
 };
@@ -310,7 +312,16 @@ extern "C" int mmdg_create(mmdg_context** out, int device) {
   std::vector<double> t64;
   std::vector<float> t32;
   build_boys_table(t64, t32);
-  if (h->boys64.upload(t64) != cudaSuccess || h->boys32.upload(t32) != cudaSuccess) {
+  std::vector<float> tdf((size_t)kBoysTabSize / kBoysRow * kBoysDfRow);
+  for (int r = 0; r < kBoysTabSize / kBoysRow; ++r)
+    for (int j = 0; j < kBoysRow; ++j) {
+      const double c = t64[(size_t)r * kBoysRow + j];
+      const float hi = float(c);
+      tdf[(size_t)r * kBoysDfRow + j] = hi;
+      tdf[(size_t)r * kBoysDfRow + kBoysRow + j] = float(c - double(hi));
+    }
+  if (h->boys64.upload(t64) != cudaSuccess || h->boys32.upload(t32) != cudaSuccess ||
+      h->boysdf.upload(tdf) != cudaSuccess) {
     delete h;
     return fail(MMDG_E_NOMEM, "mmdg_create: cannot allocate the Boys tables");
   }
@@ -844,7 +855,7 @@ extern "C" int mmdg_device_bytes(mmdg_context* h, long long* bytes) {
   if (!h || !bytes) return fail(MMDG_E_ARG, "mmdg_device_bytes: null argument");
   long long b = 0;
 #define MMDG_ADD(buf) b += (long long)(h->buf).n * (long long)sizeof(*(h->buf).p)
-  MMDG_ADD(boys64); MMDG_ADD(boys32);
+  MMDG_ADD(boys64); MMDG_ADD(boys32); MMDG_ADD(boysdf);
   MMDG_ADD(d_center); MMDG_ADD(d_exp); MMDG_ADD(d_coef);
   MMDG_ADD(d_L); MMDG_ADD(d_nprim); MMDG_ADD(d_poff); MMDG_ADD(d_func); MMDG_ADD(d_shmol); MMDG_ADD(d_shlocal);
   MMDG_ADD(d_mol_base); MMDG_ADD(d_mol_sbase); MMDG_ADD(d_mol_tbase); MMDG_ADD(d_mol_n); MMDG_ADD(d_mol_ns);

@@ -27,6 +27,9 @@ constexpr int kBoysRow = 8;         // doubles per (k, L) Taylor row (7 used)
 constexpr int kBoysExpOff = kBoysNGrid * (kBoysLMax + 1) * kBoysRow;  // exp rows after the F rows
 constexpr int kBoysTabSize = kBoysExpOff + kBoysNGrid * kBoysRow;
 constexpr double kBoysTaylorMax = 48.0 - 1.0 / 32.0;
+// the same rows as float pairs (hi, lo) for the double-float evaluation: a row is 16
+// floats, hi[0..7] then lo[0..7], with hi + lo the FP64 coefficient to ~48 bits
+constexpr int kBoysDfRow = 16;
 constexpr double kTwoPi52 = 34.986836655249725;  // 2 pi^{5/2}
 // sqrt(2 pi^{5/2}): folded into every E' coefficient by the pair kernel, so the
 // product of a bra and a ket coefficient carries the 2 pi^{5/2} of the primitive ERI
@@ -91,6 +94,7 @@ struct Geometry {
   // Boys tables
   const double* __restrict__ boys64;  // [kBoysTabSize]
   const float* __restrict__ boys32;
+  const float* __restrict__ boysdf;   // [kBoysTabSize / kBoysRow * kBoysDfRow]: (hi, lo) rows
 };
 
 // ---------------------------------------------------------------------------------
@@ -197,6 +201,116 @@ __device__ __forceinline__ void boys_eval(const float* __restrict__ tab, float T
 }
 
 // ---------------------------------------------------------------------------------
+// Double-float ("float pair") arithmetic on the FP32 pipe, after Dekker (1971) and
+// Knuth's two-sum, with the FMA giving exact products: a value is hi + lo with
+// |lo| <= ulp(hi)/2, about 48 significant bits.  Used where a result needs ~1e-14
+// relative accuracy and the FP64 pipe (1/61 of the FP32 rate here) is the bottleneck.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+// a * y + c: the Horner step
+__device__ __forceinline__ DF df_fma(DF a, DF y, DF c) {
+  const float p = a.hi * y.hi;
+  float e = fmaf(a.hi, y.hi, -p);
+  e = fmaf(a.hi, y.lo, e);
+  e = fmaf(a.lo, y.hi, e);
+  DF s = df_two_sum(p, c.hi);
+  return df_fast_two_sum(s.hi, s.lo + (e + c.lo));
+}
+
+// a finite float as a double, exactly, on the integer pipe (zero and subnormal: 0)
+__device__ __forceinline__ double f64_of_float(float x) {
+  const int b = __float_as_int(x);
+  const int e = (b >> 23) & 0xff;
+  if (e == 0) return 0.0;
+  return __hiloint2double((b & 0x80000000) | ((e + (1023 - 127)) << 20) | ((b & 0x7fffff) >> 3), (b & 7) << 29);
+}
+
+// a double as a float pair on the integer pipe: hi = the top 24 significant bits,
+// lo = the next 29 rounded to 24 (|x| below 2^-74: lo = 0; below 2^-126: 0)
+__device__ __forceinline__ DF df_of_double(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int e = (hi >> 20) & 0x7ff;
+  const int sign = hi & 0x80000000;
+  if (e < 1023 - 126) return {0.0f, 0.0f};
+  const float h = __int_as_float(sign | ((e - (1023 - 127)) << 23) | ((hi & 0xfffff) << 3) | (int)(lo >> 29));
+  float l = 0.0f;
+  if (e >= 1023 - 74) {
+    const float scale = __int_as_float((e - 1075 + 127) << 23);  // 2^(e - 1075)
+    l = __int2float_rn((int)(lo & 0x1fffffffu)) * scale;
+    l = sign ? -l : l;
+  }
+  return {h, l};
+}
+
+// sum_{n >= 1} c_n y^(n-1) over one table row (n up to 6, or 7 for an exp row), as a
+// float pair: the terms n >= 5 (below 3e-10 of the row's sum for |y| <= 1/32) in FP32,
+// n = 4..1 by double-float Horner steps
+template <int DEG>
+__device__ __forceinline__ DF df_row_tail(const float* __restrict__ row, DF y) {
+  const float4 h0 = __ldg(reinterpret_cast<const float4*>(row)), h1 = __ldg(reinterpret_cast<const float4*>(row) + 1);
+  const float4 l0 = __ldg(reinterpret_cast<const float4*>(row) + 2), l1 = __ldg(reinterpret_cast<const float4*>(row) + 3);
+  float t = DEG == 7 ? fmaf(h1.w, y.hi, h1.z) : h1.z;  // c7 y + c6, or c6
+  t = fmaf(t, y.hi, h1.y);                             // ... + c5
+  DF p{t, 0.0f};
+  p = df_fma(p, y, DF{h1.x, l1.x});
+  p = df_fma(p, y, DF{h0.w, l0.w});
+  p = df_fma(p, y, DF{h0.z, l0.z});
+  p = df_fma(p, y, DF{h0.y, l0.y});
+  return p;
+}
+
+// one Taylor row: c_0 + y * tail, the last step in FP64 (c_0 read from the FP64 row),
+// so the float pair's ~2^-47 relative error reaches the result scaled by |y| <= 1/32
+template <int DEG>
+__device__ __forceinline__ double df_row(const float* __restrict__ row, const double* __restrict__ row64, double y,
+                                         DF ydf) {
+  const DF t = df_row_tail<DEG>(row, ydf);
+  return fma(y, f64_of_float(t.hi) + f64_of_float(t.lo), __ldg(row64));
+}
+
+// Fn[0..L] for T < 48 - 1/32 from boys_eval's table with the Taylor rows evaluated
+// mostly on the FP32 pipe: per row one FP64 add and one FP64 FMA (plus y = T_k - T
+// once) instead of six FMAs; for L > 1 the exp row likewise, the downward recursion
+// stays FP64.  Relative error of a row 2.2e-16 against its FP64 Horner evaluation
+// (emulated over T < 48, L <= 4 and the exp rows).  T at or past the table takes
+// boys_eval's asymptotic branch, and so does every T when the geometry carries no
+// float-pair table (tdf null).
+template <int L>
+__device__ __forceinline__ void boys_eval_df(const float* __restrict__ tdf, const double* __restrict__ t64, double T,
+                                             double* Fn) {
+  const float Tf = f32_of_nonneg(T);
+  if (tdf == nullptr || !(Tf < float(kBoysTaylorMax))) {
+    boys_eval<L>(t64, T, Fn);
+    return;
+  }
+  const int k = __float2int_rn(Tf * 16.0f);
+  const double Tk = k == 0 ? 0.0 : f64_of_positive(float(k) * 0.0625f);  // k/16, exact
+  const double y = Tk - T;
+  const DF ydf = df_of_double(y);
+  Fn[L] = df_row<6>(tdf + (L * kBoysNGrid + k) * kBoysDfRow, t64 + (L * kBoysNGrid + k) * kBoysRow, y, ydf);
+  if (L == 1) {
+    Fn[0] = df_row<6>(tdf + k * kBoysDfRow, t64 + k * kBoysRow, y, ydf);
+  } else if (L > 1) {
+    const double eT = df_row<7>(tdf + (kBoysExpOff / kBoysRow + k) * kBoysDfRow, t64 + kBoysExpOff + k * kBoysRow, y,
+                                ydf);
+    const double T2 = T + T;
+#pragma unroll
+    for (int m = L; m > 0; --m) Fn[m - 1] = fma(T2, Fn[m], eT) * (1.0 / double(2 * m - 1));
+  }
+}
+
+// ---------------------------------------------------------------------------------
 // per-quartet context handed to the generated class code
 template <typename Real>
 struct Ctx;
@@ -264,7 +378,7 @@ struct Ctx<double> {
         const double alpha = pq * (rr * rr);
         const double T = alpha * r2;
         double F[L + 1];
-        boys_eval<L>(g->boys64, T, F);
+        boys_eval_df<L>(g->boysdf, g->boys64, T, F);
         double c = rr;  // 2 pi^{5/2} is folded into the E' coefficients
         const double m2a = -2.0 * alpha;
 #pragma unroll

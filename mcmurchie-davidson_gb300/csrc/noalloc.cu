@@ -329,6 +329,7 @@ extern "C" int mmdg_eri_tensor_noalloc(int nshell, const int* shell_L, const int
   g.mol_base = dMolBase;
   g.mol_n = dMolN;
   g.boys64 = reinterpret_cast<const double*>(base + kOffBoys);
+  g.boysdf = nullptr;  // the static scratch holds the FP64 rows only: boys_eval_df uses them
   TensorArgs t{out};
   for (const ClassEntry& ce : kClasses) {
     const int cb = ce.la * (ce.la + 1) / 2 + ce.lb, ck = ce.lc * (ce.lc + 1) / 2 + ce.ld;

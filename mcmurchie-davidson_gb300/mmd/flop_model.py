@@ -135,20 +135,33 @@ def boys_flops(L: int, asymptotic: bool) -> int:
     return RSQRT_FLOPS + 2 + (1 + 3 * L if L > 4 else 2 * L)
 
 
+def boys_df_flops(L: int) -> int:
+    """FP64 FLOPs of boys_eval_df<L> (md_device.cuh), the near branch of L <= 4: y =
+    T_k - T (1), per Taylor row a conversion sum (1) and the last Horner step as an FMA
+    (2) -- the other steps run as float pairs on the FP32 pipe -- and for L > 1 the exp
+    row likewise, 2T and the downward recursion (an FMA and a product per order)."""
+    if L == 0:
+        return 1 + 3
+    if L == 1:
+        return 1 + 3 + 3
+    return 1 + 3 + 3 + 1 + 3 * L
+
+
 def r0_flops(L: int, asymptotic: bool) -> int:
     """hermite_r0_pp<L> (md_device.cuh).  L <= 4: P - Q (3), |PQ|^2 (5), pq, p + q and
     pq |PQ|^2 (3), one rsqrt_dd; near (T < 48): alpha (2), T (1), Boys and the prefactor
     powers R^(n) = (-2 alpha)^n F_n / sqrt(p+q) (-2 alpha once for L > 0, one product per
     order and one per step of the power); far: the point-charge form R^(0) = c / sqrt(pq
     |PQ|^2) (1) and, for L > 0, -1/|PQ|^2 (2), R^(1) (1) and two products per further
-    order.  L >= 5 (the warp kernel): P - Q, |PQ|^2, p + q, rsqrt_dd(p + q), alpha (3),
-    T, Boys (either branch), the prefactor powers."""
+    order; near lanes evaluate the Boys function by boys_eval_df.  L >= 5 (the warp
+    kernel): P - Q, |PQ|^2, p + q, rsqrt_dd(p + q), alpha (3), T, Boys (either branch of
+    boys_eval), the prefactor powers."""
     pref = 1 if L == 0 else 1 + (2 * L + 1)
     if L <= 4:
         common = 3 + 5 + 3 + RSQRT_FLOPS
         if asymptotic:
             return common + (1 if L == 0 else 2 * L + 2)
-        return common + 2 + 1 + boys_flops(L, False) + pref
+        return common + 2 + 1 + boys_df_flops(L) + pref
     return 3 + 5 + 1 + RSQRT_FLOPS + 3 + 1 + boys_flops(L, asymptotic) + pref
 
 

@@ -278,10 +278,11 @@ def test_issued_and_useful_flop_counts():
         if F.fock_kernel(c) == "thread" and F._thread_config(tuple(c))[0] == 1:
             assert i == u
     assert F.fock_kernel((2, 2, 2, 2)) == "warp" and F.fock_kernel((1, 0, 0, 0)) == "thread"
-    # (ss|ss), near: P-Q 3, |PQ|^2 5, pq, p+q, pq|PQ|^2 3, rsqrt 8, alpha 2, T 1, Boys 13,
-    # prefactor 1; far: the common part and one product; ket 2 per primitive quartet,
-    # bra 2 per bra pass, 6 per digested function quartet
-    assert F.r0_flops(0, False) == 3 + 5 + 3 + 8 + 2 + 1 + 13 + 1
+    # (ss|ss), near: P-Q 3, |PQ|^2 5, pq, p+q, pq|PQ|^2 3, rsqrt 8, alpha 2, T 1, Boys on
+    # float pairs 4 (y, one conversion sum, the last FMA), prefactor 1; far: the common
+    # part and one product; ket 2 per primitive quartet, bra 2 per bra pass, 6 per
+    # digested function quartet
+    assert F.r0_flops(0, False) == 3 + 5 + 3 + 8 + 2 + 1 + 4 + 1
     assert F.r0_flops(0, True) == 3 + 5 + 3 + 8 + 1
     # (ps|ss) far: -1/|PQ|^2 2, R0 1, R1 1; (dd|dd) keeps the Boys-function form
     assert F.r0_flops(1, True) == 19 + 4
