@@ -566,21 +566,25 @@ def consumers_bench():
     return out
 
 
-# The chosen form's stopping rule: ||P - P_old|| < 1e-5, then one polish build.  The
+# The chosen form's stopping rule: ||P - P_old|| < 3e-5, then one polish build.  The
 # polished energy E(P) = tr((H + F(P)) P) + E_nuc is stationary at the SCF solution,
-# so its error is second order in the density error: measured 8e-12 Eh on (H2O)16
-# 6-31G** and within 1e-8 Eh of the reference's own energies on the held-out (H2O)8
+# so its error is second order in the density error.  Measured on three (H2O)16
+# 6-31G** geometries (seeds 16-18, learned guess; against the plain path's polished
+# energy at conver 1e-10): stopping at 3e-4 / 1e-4 / 3e-5 / 1e-5 took 7 / 8-9 / 9 /
+# 10-11 iterations with energy errors up to 6.3e-9 / 3.5e-10 / 6.1e-11 / 6.4e-12 Eh;
+# 3e-5 keeps a 160-fold margin to the 1e-8 Eh target.  The same rule holds the
+# held-out (H2O)8 within 1e-8 Eh of the reference's own energies
 # (tests/test_gpu_reference_energies.py).  The plain path keeps the reference's rule
 # (||dP|| < 1e-8 with the reference's first-order energy formula).  The iterations take
 # FP32 below Schwarz 1e-1 (each such ERI off by at most 5e-7 x 1e-1; the density only
-# has to reach 1e-5), the polish build FP32 below 1e-5 (at most 5e-12 per ERI).
+# has to reach 3e-5), the polish build FP32 below 1e-5 (at most 5e-12 per ERI).
 # Measured on (H2O)16 (learned guess, 10 iterations; energy against the plain FP64
 # path's polished energy at conver 1e-10): FP32 below 1e-3 / 1e-2 / 1e-1 / 1 in the
 # iterations 0.419 / 0.413 / 0.392 / 0.378 s, energy error 0.9 / 1.0 / 1.1 / 11 e-11
 # Eh; polish build FP32 below 0 / 1e-7 / 1e-6 / 1e-5 / 1e-4: 40.4 / 31.4 / 29.0 /
 # 26.9 / 24.5 ms, energy error 0.3 / 0.6 / 0.5 / 0.09 / -2.5 e-11 Eh.
 CHOSEN_FP32_BELOW = 1e-1
-CHOSEN_CONVER = 1e-5
+CHOSEN_CONVER = 3e-5
 CHOSEN_POLISH_FP32_BELOW = 1e-5
 # Eigensolver of the chosen form's iterations: the dense host solve of all N orbitals.
 # The occupied-subspace solver (mmd.scf.OccupiedSubspace: Chebyshev-filtered subspace

@@ -51,7 +51,7 @@ def test_combined_form_matches_the_reference_energies():
 
 def test_chosen_single_molecule_form_matches_the_reference_energies():
     """The single-molecule chosen form of the benchmark -- learned guess, FP32 below
-    Schwarz 1e-1, stop at ||dP|| < 1e-5, occupied orbitals by subspace iteration, polish
+    Schwarz 1e-1, stop at ||dP|| < 3e-5, occupied orbitals by subspace iteration, polish
     build (FP32 below 1e-5) -- against the reference's energies, and the same run with
     the dense eigensolver within 1e-9 Eh of it."""
     from mmd import guess as G
@@ -64,7 +64,7 @@ def test_chosen_single_molecule_form_matches_the_reference_energies():
         for eig in ("subspace", "dense"):
             mol = Molecule(g, "6-31g")
             P0 = G.predict_density(net, mol)
-            out[eig] = float(mol.RHF(doPrint=False, direct=True, fp32_below=1e-1, guess=P0, conver=1e-5, polish=True,
+            out[eig] = float(mol.RHF(doPrint=False, direct=True, fp32_below=1e-1, guess=P0, conver=3e-5, polish=True,
                                      polish_fp32_below=1e-5, eigensolver=eig))
             assert mol.is_converged
             if eig == "subspace":
