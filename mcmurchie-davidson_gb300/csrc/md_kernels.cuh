@@ -167,17 +167,17 @@ __global__ void __launch_bounds__(kMaxFockBlock) k_fock(Geometry g, FockArgs f, 
   // block size: kThreads for classes with shared-memory R tables, else 64..256 (tile),
   // a multiple of 32 either way, so every warp is full
   const long long nthreads = (long long)gridDim.x * blockDim.x;
-  const bool kDynamic = sizeof(Real) == 8 && total >= 8 * nthreads;
+  const bool dynamic = sizeof(Real) == 8 && total >= 8 * nthreads;
   const unsigned lane = threadIdx.x & 31u;
   unsigned long long base = 0, next = 0;
   long long sidx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (kDynamic) {
+  if (dynamic) {
     if (lane == 0) base = atomicAdd(f.work, 32ull);
     base = __shfl_sync(0xffffffffu, base, 0);
   }
   for (;;) {
     long long idx;
-    if (kDynamic) {
+    if (dynamic) {
       if (base >= (unsigned long long)total) break;  // warp-uniform
       if (lane == 0) next = atomicAdd(f.work, 32ull);  // the next claim, in flight during this one
       idx = (long long)base + lane;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kMaxFockBlock) k_fock(Geometry g, FockArgs f, 
         nas += c.nasym;
       }
     }
-    if (kDynamic) base = __shfl_sync(0xffffffffu, next, 0);
+    if (dynamic) base = __shfl_sync(0xffffffffu, next, 0);
     else sidx += nthreads;
   }
   if (f.counters) {
