@@ -357,3 +357,67 @@ def test_occupied_subspace_iteration_matches_the_dense_solve():
     if r is not None:
         wg = np.linalg.eigvalsh(G + G.T)
         assert np.abs(r[0] - wg[:nocc]).max() < 1e-8
+
+
+def test_float_pair_boys_rows_match_fp64_horner():
+    """The float-pair evaluation of the Boys Taylor rows (md_device.cuh, boys_eval_df),
+    restated in numpy float32 with exact FMA products: the tail n >= 5 in FP32, the
+    steps n = 4..1 as float pairs, the last step c_0 + y * tail in FP64.  Over T < 48,
+    orders 0..4 and the exp rows it stays within 4e-16 of the FP64 Horner value of the
+    same table row (the device table is the host table, split into (hi, lo) floats)."""
+    import ctypes
+    from mmd import _native
+    n = _native.lib().mmdg_boys_table(None, 0)
+    tab = np.zeros(n)
+    _native.lib().mmdg_boys_table(tab.ctypes.data_as(ctypes.c_void_p), n)
+    NG, ROW, LMAX = 768, 8, 8
+    EXPOFF = NG * (LMAX + 1) * ROW
+    f32 = np.float32
+
+    def fmaf(a, b, c):  # float products are exact in float64
+        return f32(np.float64(a) * np.float64(b) + np.float64(c))
+
+    def two_sum(a, b):
+        s = f32(a + b)
+        bb = f32(s - a)
+        return s, f32(f32(a - f32(s - bb)) + f32(b - bb))
+
+    def df_fma(ah, al, yh, yl, ch, cl):
+        p = f32(ah * yh)
+        e = fmaf(al, yh, fmaf(ah, yl, fmaf(ah, yh, -p)))
+        sh, sl = two_sum(p, ch)
+        s = f32(sh + f32(sl + f32(e + cl)))
+        return s, f32(f32(sl + f32(e + cl)) - f32(s - sh))
+
+    def split(x):
+        h = f32(x)
+        return h, f32(x - np.float64(h))
+
+    def row_df(row, y, deg):
+        m, e = np.frexp(y)
+        yh = f32(np.trunc(m * 2 ** 24) / 2 ** 24 * 2.0 ** e) if y != 0 else f32(0)
+        yl = f32(y - np.float64(yh))
+        hl = [split(c) for c in row]
+        t = fmaf(hl[7][0], yh, hl[6][0]) if deg == 7 else hl[6][0]
+        ph, pl = fmaf(t, yh, hl[5][0]), f32(0)
+        for j in (4, 3, 2, 1):
+            ph, pl = df_fma(ph, pl, yh, yl, hl[j][0], hl[j][1])
+        return y * (np.float64(ph) + np.float64(pl)) + row[0]
+
+    def row_64(row, y, deg):
+        f = row[deg]
+        for j in range(deg - 1, -1, -1):
+            f = f * y + row[j]
+        return f
+
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for T in rng.uniform(0.0, 47.9, 120):
+        k = min(int(np.rint(np.float32(T) * 16)), NG - 1)
+        y = k / 16.0 - T
+        rows = [(tab[(L * NG + k) * ROW:(L * NG + k + 1) * ROW], 6) for L in range(5)]
+        rows.append((tab[EXPOFF + k * ROW:EXPOFF + (k + 1) * ROW], 7))
+        for row, deg in rows:
+            ref = row_64(row, y, deg)
+            worst = max(worst, abs(row_df(row, y, deg) - ref) / abs(ref))
+    assert worst < 4e-16, worst
