@@ -297,8 +297,7 @@ def gen_class_compact(la, lb, lc, ld):
     o.append(f"#pragma unroll 1")
     o.append(f"          for (int t = t0; t < t1; ++t) {{")
     o.append(f"            const unsigned h = kTH_{s}[t];")
-    o.append(f"            const Real ev = ek[kTO_{s}[t]];")
-    o.append(f"            const Real e = (h >> 15) ? -ev : ev;")
+    o.append(f"            const Real e = mmdg::flip_sign(ek[kTO_{s}[t]], (int)(h >> 15));  // sign on the integer pipe")
     o.append(f"            const unsigned short* __restrict__ cb = kCB_{s} + (h & 0x7fffu) * {len(hp)};")
     o.append("            " + " ".join(f"w{k} = fma(e, Rs[cb[{k}] * RS], w{k});" for k in range(len(hp))))
     o.append(f"          }}")

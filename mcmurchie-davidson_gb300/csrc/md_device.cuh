@@ -66,6 +66,16 @@ __device__ __forceinline__ double rsqrt_dd(double x) {
   return fma(y0, e * fma(e, 0.375, 0.5), y0);
 }
 
+// (-1)^s x by an integer XOR of the sign bit.  A select between x and -x compiles to
+// an FP64 negation (an add) per term, which costs the FP64 pipe as much as the FMA it
+// feeds; the XOR runs on the integer pipe.
+__device__ __forceinline__ double flip_sign(double x, int s) {
+  return __hiloint2double(__double2hiint(x) ^ (int)((unsigned)s << 31), __double2loint(x));
+}
+__device__ __forceinline__ float flip_sign(float x, int s) {
+  return __int_as_float(__float_as_int(x) ^ (int)((unsigned)s << 31));
+}
+
 // ---------------------------------------------------------------------------------
 // geometry shared by every kernel
 struct Geometry {

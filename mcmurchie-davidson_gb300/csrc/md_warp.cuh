@@ -35,16 +35,6 @@ namespace mmdg {
 constexpr int kWarps = kThreads / 32;
 constexpr int kItem = 8;  // most list quartets per warp work item (k_fock_warp)
 
-// (-1)^s x by an integer XOR of the sign bit.  A select between x and -x compiles to
-// an FP64 negation (an add) per term, which costs the FP64 pipe as much as the FMA it
-// feeds; the XOR runs on the integer pipe.
-__device__ __forceinline__ double flip_sign(double x, int s) {
-  return __hiloint2double(__double2hiint(x) ^ (int)((unsigned)s << 31), __double2loint(x));
-}
-__device__ __forceinline__ float flip_sign(float x, int s) {
-  return __int_as_float(__float_as_int(x) ^ (int)((unsigned)s << 31));
-}
-
 __device__ __forceinline__ int herm_index(int t, int u, int v) {
   const int n = t + u + v, m = n - t;
   return n * (n + 1) * (n + 2) / 6 + m * (m + 1) / 2 + (m - u);
