@@ -53,17 +53,39 @@ __device__ __forceinline__ double f64_of_positive(float y) {
   return __hiloint2double((((b >> 23) + (1023 - 127)) << 20) | ((b & 0x7fffff) >> 3), (b & 7) << 29);
 }
 
+// a finite float as a double, exactly, on the integer pipe (zero and subnormal: 0)
+__device__ __forceinline__ double f64_of_float(float x) {
+  const int b = __float_as_int(x);
+  const int e = (b >> 23) & 0xff;
+  if (e == 0) return 0.0;
+  return __hiloint2double((b & 0x80000000) | ((e + (1023 - 127)) << 20) | ((b & 0x7fffff) >> 3), (b & 7) << 29);
+}
+
+// a double as a float rounded toward zero, sign kept, on the integer pipe (relative
+// error below 2^-23; magnitudes below the normal float range give 0)
+__device__ __forceinline__ float f32_of_double_tz(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int fe = min(((hi >> 20) & 0x7ff) - (1023 - 127), 254);
+  return fe <= 0 ? 0.0f
+                 : __int_as_float((hi & 0x80000000) | (fe << 23) | ((hi & 0xfffff) << 3) | (int)(lo >> 29));
+}
+
 // 1/sqrt(x) for a positive double whose magnitude is within the normal float range:
 // the single-precision estimate y0 = rsqrtf(x) (special-function unit; x and y0
 // moved between formats on the integer pipe) and one third-order step of the
 // Newton/Householder iteration for the inverse square root,
-//     e = 1 - x y0^2,   y = y0 (1 + e/2 + 3 e^2/8),
+//     e = 1 - x y0^2,   y = y0 (1 + e/2 + 3 e^2/8) = y0 + (y0/2) (e + (3e/4) e),
 // whose error is 5/16 e^3 + O(e^4); |e| < 2^-20 leaves it far below double rounding.
-// Five FP64 instructions.
+// The factor 3e/4 only scales a term below 2^-40 of the result, so it is taken from
+// the FP32 pipe (24 bits), and y0/2 is exact in FP32: four FP64 instructions (a
+// product and three FMAs), the same rounding as the all-FP64 step.
 __device__ __forceinline__ double rsqrt_dd(double x) {
-  const double y0 = f64_of_positive(rsqrtf(f32_of_nonneg(x)));
+  const float y0f = rsqrtf(f32_of_nonneg(x));
+  const double y0 = f64_of_positive(y0f);
   const double e = fma(-x, y0 * y0, 1.0);  // y0 has 24 significant bits: y0^2 is exact
-  return fma(y0, e * fma(e, 0.375, 0.5), y0);
+  const double b = fma(f64_of_float(0.75f * f32_of_double_tz(e)), e, e);  // e + 3e^2/4
+  return fma(f64_of_positive(0.5f * y0f), b, y0);
 }
 
 // (-1)^s x by an integer XOR of the sign bit.  A select between x and -x compiles to
@@ -237,14 +259,6 @@ __device__ __forceinline__ DF df_fma(DF a, DF y, DF c) {
   return df_fast_two_sum(s.hi, s.lo + (e + c.lo));
 }
 
-// a finite float as a double, exactly, on the integer pipe (zero and subnormal: 0)
-__device__ __forceinline__ double f64_of_float(float x) {
-  const int b = __float_as_int(x);
-  const int e = (b >> 23) & 0xff;
-  if (e == 0) return 0.0;
-  return __hiloint2double((b & 0x80000000) | ((e + (1023 - 127)) << 20) | ((b & 0x7fffff) >> 3), (b & 7) << 29);
-}
-
 // a double as a float pair on the integer pipe: hi = the top 24 significant bits,
 // lo = the next 29 rounded to 24 (|x| below 2^-74: lo = 0; below 2^-126: 0)
 __device__ __forceinline__ DF df_of_double(double x) {
@@ -359,8 +373,13 @@ struct Ctx<double> {
   //   terms are below 5e-15 relative for n <= 4) turns R^(n) into the point-charge
   //   form R^(0) = sqrt(pi)/2 / (sqrt(pq) |PQ|), R^(n) = -(2n-1) R^(n-1) / |PQ|^2,
   //   which needs 1/sqrt(pq |PQ|^2) and no Boys function or alpha at all.
-  // Both sides take their one reciprocal square root from the same rsqrt_dd call
-  // (argument p+q or pq |PQ|^2), so a warp whose lanes straddle T = 48 issues it once.
+  // Both sides are one product chain, R^(n) = rr M^n B_n, with
+  //   near: rr = 1/sqrt(p+q),      M = -2 pq rr^2 = -2 alpha, B_n = F_n(T);
+  //   far:  rr = 1/sqrt(pq |PQ|^2), M = -pq rr^2 = -1/|PQ|^2,  B_n = (2n-1)!! sqrt(pi)/2,
+  // so a warp whose lanes straddle T = 48 (most warps of the s and p classes: far
+  // primitive quartets outnumber near ones about 4 to 1 in water clusters) issues the
+  // reciprocal square root and the chain once, and only T and the Boys rows on the
+  // near side; M's sign and factor 2 are set on the integer pipe.
   // A near lane whose FP64 T lands past the table still gets the asymptotic form
   // inside boys_eval (its own test), so the table is never read out of range.
   template <int L>
@@ -375,26 +394,28 @@ struct Ctx<double> {
       const float Tf = __fdividef(f32_of_nonneg(pqr2), f32_of_nonneg(s));
       const bool far = Tf >= float(kBoysTaylorMax);
       const double rr = rsqrt_dd(far ? pqr2 : s);
+      const double pqrr2 = pq * (rr * rr);  // near: alpha; far: 1/|PQ|^2
+      double B[L + 1];
       if (far) {
         ++nasym;
-        Rn[0] = kHalfSqrtPi * rr;
-        if (L > 0) {
-          const double nir2 = (rr * rr) * -pq;  // -1/|PQ|^2
-          Rn[1] = Rn[0] * nir2;
-#pragma unroll
-          for (int n = 2; n <= L; ++n) Rn[n] = Rn[n - 1] * (double(2 * n - 1) * nir2);
-        }
-      } else {
-        const double alpha = pq * (rr * rr);
-        const double T = alpha * r2;
-        double F[L + 1];
-        boys_eval_df<L>(g->boysdf, g->boys64, T, F);
-        double c = rr;  // 2 pi^{5/2} is folded into the E' coefficients
-        const double m2a = -2.0 * alpha;
+        double f = kHalfSqrtPi;
 #pragma unroll
         for (int n = 0; n <= L; ++n) {
-          Rn[n] = c * F[n];
-          c *= m2a;
+          B[n] = f;
+          f *= double(2 * n + 1);  // compile-time constants
+        }
+      } else {
+        boys_eval_df<L>(g->boysdf, g->boys64, pqrr2 * r2, B);
+      }
+      double c = rr;  // 2 pi^{5/2} is folded into the E' coefficients
+      Rn[0] = c * B[0];
+      if (L > 0) {
+        const unsigned hm = ((unsigned)__double2hiint(pqrr2) ^ 0x80000000u) + (far ? 0u : 0x00100000u);
+        const double M = __hiloint2double((int)hm, __double2loint(pqrr2));
+#pragma unroll
+        for (int n = 1; n <= L; ++n) {
+          c *= M;
+          Rn[n] = c * B[n];
         }
       }
       return;

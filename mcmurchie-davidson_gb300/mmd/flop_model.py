@@ -116,7 +116,7 @@ def _gm():
     return _gen_md()
 
 
-RSQRT_FLOPS = 8  # rsqrt_dd: y0^2, two FMAs, one product, one FMA (md_device.cuh)
+RSQRT_FLOPS = 7  # rsqrt_dd: y0^2 and three FMAs (md_device.cuh; 3e/4 and y0/2 from FP32)
 
 
 def boys_flops(L: int, asymptotic: bool) -> int:
@@ -149,19 +149,19 @@ def boys_df_flops(L: int) -> int:
 
 def r0_flops(L: int, asymptotic: bool) -> int:
     """hermite_r0_pp<L> (md_device.cuh).  L <= 4: P - Q (3), |PQ|^2 (5), pq, p + q and
-    pq |PQ|^2 (3), one rsqrt_dd; near (T < 48): alpha (2), T (1), Boys and the prefactor
-    powers R^(n) = (-2 alpha)^n F_n / sqrt(p+q) (-2 alpha once for L > 0, one product per
-    order and one per step of the power); far: the point-charge form R^(0) = c / sqrt(pq
-    |PQ|^2) (1) and, for L > 0, -1/|PQ|^2 (2), R^(1) (1) and two products per further
-    order; near lanes evaluate the Boys function by boys_eval_df.  L >= 5 (the warp
-    kernel): P - Q, |PQ|^2, p + q, rsqrt_dd(p + q), alpha (3), T, Boys (either branch of
-    boys_eval), the prefactor powers."""
+    pq |PQ|^2 (3), one rsqrt_dd, then the chain R^(n) = rr M^n B_n shared by both sides:
+    R^(0) (1) and two products per order n >= 1; M = -2 pq rr^2 or -pq rr^2 needs pq rr^2
+    (2; sign and factor 2 on the integer pipe), which for L = 0 only the near side
+    computes; near (T < 48) adds T (1) and the Boys rows by boys_eval_df, far lanes take
+    constant B_n.  L >= 5 (the warp kernel): P - Q, |PQ|^2, p + q, rsqrt_dd(p + q),
+    alpha (3), T, Boys (either branch of boys_eval), the prefactor powers."""
     pref = 1 if L == 0 else 1 + (2 * L + 1)
     if L <= 4:
         common = 3 + 5 + 3 + RSQRT_FLOPS
+        chain = 1 + 2 * L
         if asymptotic:
-            return common + (1 if L == 0 else 2 * L + 2)
-        return common + 2 + 1 + boys_df_flops(L) + pref
+            return common + (0 if L == 0 else 2) + chain
+        return common + 2 + 1 + boys_df_flops(L) + chain
     return 3 + 5 + 1 + RSQRT_FLOPS + 3 + 1 + boys_flops(L, asymptotic) + pref
 
 

@@ -278,15 +278,17 @@ def test_issued_and_useful_flop_counts():
         if F.fock_kernel(c) == "thread" and F._thread_config(tuple(c))[0] == 1:
             assert i == u
     assert F.fock_kernel((2, 2, 2, 2)) == "warp" and F.fock_kernel((1, 0, 0, 0)) == "thread"
-    # (ss|ss), near: P-Q 3, |PQ|^2 5, pq, p+q, pq|PQ|^2 3, rsqrt 8, alpha 2, T 1, Boys on
-    # float pairs 4 (y, one conversion sum, the last FMA), prefactor 1; far: the common
-    # part and one product; ket 2 per primitive quartet, bra 2 per bra pass, 6 per
-    # digested function quartet
-    assert F.r0_flops(0, False) == 3 + 5 + 3 + 8 + 2 + 1 + 4 + 1
-    assert F.r0_flops(0, True) == 3 + 5 + 3 + 8 + 1
-    # (ps|ss) far: -1/|PQ|^2 2, R0 1, R1 1; (dd|dd) keeps the Boys-function form
-    assert F.r0_flops(1, True) == 19 + 4
-    assert F.r0_flops(8, True) == 3 + 5 + 1 + 8 + 3 + 1 + F.boys_flops(8, True) + 18
+    # (ss|ss), near: P-Q 3, |PQ|^2 5, pq, p+q, pq|PQ|^2 3, rsqrt 7 (a product and three
+    # FMAs), alpha 2, T 1, Boys on float pairs 4 (y, one conversion sum, the last FMA),
+    # R0 1; far: the common part and R0; ket 2 per primitive quartet, bra 2 per bra
+    # pass, 6 per digested function quartet
+    assert F.r0_flops(0, False) == 3 + 5 + 3 + 7 + 2 + 1 + 4 + 1
+    assert F.r0_flops(0, True) == 3 + 5 + 3 + 7 + 1
+    # (ps|ss): near and far share R0, rr M, R1 (3) and pq rr^2 (2); near adds T and two
+    # Boys rows; (dd|dd) keeps the Boys-function form
+    assert F.r0_flops(1, True) == 18 + 2 + 3
+    assert F.r0_flops(1, False) == 18 + 2 + 1 + F.boys_df_flops(1) + 3
+    assert F.r0_flops(8, True) == 3 + 5 + 1 + 7 + 3 + 1 + F.boys_flops(8, True) + 18
     assert F.useful_flops((0, 0, 0, 0), [1, 1, 1, 1, 0]) == F.r0_flops(0, False) + 2 + 2 + 6
     assert F.boys_flops(3, True) < F.boys_flops(3, False)
     # the recursion counts 1 FLOP for a first step, 2 for fma(X, R1, R2) (m = 2) and 3
@@ -421,3 +423,44 @@ def test_float_pair_boys_rows_match_fp64_horner():
             ref = row_64(row, y, deg)
             worst = max(worst, abs(row_df(row, y, deg) - ref) / abs(ref))
     assert worst < 4e-16, worst
+
+
+def test_rsqrt_step_restated_equals_the_fp64_step():
+    """rsqrt_dd (md_device.cuh) restated on the CPU with exact FMAs: from the FP32 seed
+    y0 (correctly rounded, and 1 or 2 ulp off either way, as CUDA's rsqrtf may be) and
+    e = 1 - x y0^2, the step y0 + (y0/2)(e + (3e/4) e) with 3e/4 taken in FP32 gives the
+    same double as the all-FP64 step y0 + y0 e (1/2 + 3e/8), within 1 ulp of 1/sqrt(x),
+    over p + q of primitive pairs, pq |PQ|^2 of far quartets and T >= 48."""
+    from fractions import Fraction
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    f32 = np.float32
+
+    def fma(a, b, c):  # one rounding, as the device FMA
+        return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+    def f32_tz(x):  # md_device.cuh f32_of_nonneg / f32_of_double_tz: toward zero
+        m, ex = np.frexp(abs(x))
+        v = np.copysign(np.floor(m * 2.0 ** 24) / 2.0 ** 24 * 2.0 ** ex, x)
+        return f32(v) if abs(v) >= 2.0 ** -126 else f32(0)
+
+    def seed(x, k):
+        y = f32(1.0 / np.sqrt(np.float64(f32_tz(x))))
+        for _ in range(abs(k)):
+            y = np.nextafter(y, f32(np.inf) if k > 0 else f32(0))
+        return y
+
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([10.0 ** rng.uniform(-2, 11, 400), rng.uniform(0.1, 100.0, 400),
+                         [1.0, 2.0, 4.0, 0.25, 48.0, 47.96875, 123456.789]])
+    for x in xs:
+        exact = float(1 / mp.sqrt(mp.mpf(float(x))))
+        for k in (-2, -1, 0, 1, 2):
+            y0f = seed(x, k)
+            y0 = float(y0f)
+            e = fma(-x, y0 * y0, 1.0)
+            assert abs(e) < 2.0 ** -20
+            new = fma(float(f32(0.5) * y0f), fma(float(f32(f32(0.75) * f32_tz(e))), e, e), y0)
+            old = fma(y0, e * fma(e, 0.375, 0.5), y0)
+            assert new == old
+            assert abs(new - exact) <= np.spacing(exact)
