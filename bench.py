@@ -55,10 +55,10 @@ FQ_PER_BUILD = 198282802.0
 # launch 5 of k_fock<MD_1000> (an early Fock build of the warm-up SCF) in one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum; summary and command in
 # profiles/k_fock_1000_full_h2o16.md).
-DRAM_BYTES_PER_LAUNCH = {"1000": 50.19e6}
+DRAM_BYTES_PER_LAUNCH = {"1000": 50.20e6}
 # FP64-pipe busy fraction of the same launch over its elapsed cycles
 # (sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_elapsed, same capture)
-FP64_PIPE_BUSY = {"1000": 0.844}
+FP64_PIPE_BUSY = {"1000": 0.846}
 
 
 def _env():
