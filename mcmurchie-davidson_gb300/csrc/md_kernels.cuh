@@ -4,11 +4,13 @@
 // walks every candidate (bra shell pair, ket shell pair) of the class and appends
 // the survivors of the Schwarz x density bound to bucketed quartet lists (buckets
 // keyed by the primitive-count groups of the two pairs, FP64 and FP32 lists); then
-// k_fock, a persistent grid-stride kernel, evaluates the list, one thread per
-// (quartet, ket chunk), chunk-major, so a warp shares its code path and, inside a
-// bucket, its primitive trip counts.  The compact high-L classes have a
-// warp-cooperative Fock kernel of their own (md_warp.cuh).  The ERI tensor, the
-// Schwarz table and listed quartets use one thread per shell quartet.
+// k_fock, a persistent kernel, evaluates the list, one thread per (quartet, ket
+// chunk), chunk-major, so a warp shares its code path and, inside a bucket, its
+// primitive trip counts.  Short lists and FP32 lists are split by grid stride; long
+// FP64 lists are handed out 32 quartets per warp from an atomic counter, so the SMs
+// finish together.  The classes above L = 4 have a warp-cooperative Fock kernel of
+// their own (md_warp.cuh).  The ERI tensor, the Schwarz table and listed quartets
+// use one thread per shell quartet.
 #pragma once
 #include "md_device.cuh"
 #include "md_gen.cuh"

@@ -23,6 +23,12 @@ keyword arguments (all default to the reference's behaviour):
 * ``guess_fallback``  with a guess: revert to the core guess when the DIIS error
   grows for 3 consecutive iterations;
 * ``maxiter``     iteration cap (reference: 100);
+* ``polish``      the final energy from one non-incremental Fock build of the
+  converged density (second order in the density error); ``polish_fp32_below`` lets
+  that build run in FP32 below its own, smaller threshold;
+* ``eigensolver``  "dense" (all eigenpairs every iteration, as the reference) or
+  "subspace" (occupied orbitals by Chebyshev-filtered subspace iteration between
+  iterations, all eigenpairs once at the end; ``OccupiedSubspace``);
 * ``process_group``  a torch.distributed group with one rank per GPU: each rank
   digests its share of the shell quartets and one all-reduce of G completes every
   Fock build (``mmd.distributed``); the rest of the SCF is replicated.
