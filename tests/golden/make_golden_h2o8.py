@@ -2,7 +2,7 @@
 """Reference energies of held-out seeded (H2O)8 / 6-31G clusters, from the reference.
 
 The combined form (learned guess + FP32 below a Schwarz threshold + FP64 polish) and
-the batched SCF are judged against these: the reference's own conventional RHF
+the batched SCF are checked against these: the reference's own conventional RHF
 (mmd/scf.py:10-80 with the ERI tensor of its compiled Cython doERIs,
 cython/twoe.pyx:12-31) converged to conver = 1e-12, on the clusters
 ``water_cluster(8, seed=900000 + k)`` for k = 0..7 -- the first eight of the 64
