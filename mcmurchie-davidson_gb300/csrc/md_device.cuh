@@ -34,7 +34,7 @@ constexpr double kTwoPi52 = 34.986836655249725;  // 2 pi^{5/2}
 // sqrt(2 pi^{5/2}): folded into every E' coefficient by the pair kernel, so the
 // product of a bra and a ket coefficient carries the 2 pi^{5/2} of the primitive ERI
 // (cython/twoe.pyx:93) and the quartet code multiplies by 1/sqrt(p+q) only
-constexpr double kSqrtTwoPi52 = 5.9149671727955846;
+constexpr double kSqrtTwoPi52 = 5.914967172795613;
 constexpr double kHalfSqrtPi = 0.88622692545275801;
 
 // A non-negative double as a float rounded toward zero, from its bit pattern on the

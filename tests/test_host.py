@@ -464,3 +464,31 @@ def test_rsqrt_step_restated_equals_the_fp64_step():
             old = fma(y0, e * fma(e, 0.375, 0.5), y0)
             assert new == old
             assert abs(new - exact) <= np.spacing(exact)
+
+
+def test_device_constants_are_correctly_rounded():
+    """The mathematical constants written as literals in the CUDA sources equal the
+    correctly rounded doubles of their values (a digit off in sqrt(2 pi^{5/2}), which
+    every E' coefficient carries, shifts every ERI by the same relative amount)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    csrc = os.path.join(REPO, "mcmurchie-davidson_gb300", "csrc")
+
+    def literal(fname, pattern):
+        with open(os.path.join(csrc, fname)) as f:
+            m = re.search(pattern, f.read())
+        assert m, (fname, pattern)
+        return float(m.group(1))
+
+    num = r"([0-9]+\.[0-9]+(?:[eE][-+]?[0-9]+)?)"
+    cases = [
+        ("md_device.cuh", r"kTwoPi52 = " + num, 2 * mp.pi ** mp.mpf(2.5)),
+        ("md_device.cuh", r"kSqrtTwoPi52 = " + num, mp.sqrt(2 * mp.pi ** mp.mpf(2.5))),
+        ("md_device.cuh", r"kHalfSqrtPi = " + num, mp.sqrt(mp.pi) / 2),
+        ("capi.cu", r"comp_norm\(int l\) \{ return l >= 2 \? " + num, 1 / mp.sqrt(3)),
+        ("grad.cu", r"comp_norm\(int l\) \{ return l >= 2 \? " + num, 1 / mp.sqrt(3)),
+        ("capi.cu", r"const double PI = " + num, mp.pi),
+        ("grad.cu", r"kPi = " + num, mp.pi),
+    ]
+    for fname, pattern, exact in cases:
+        assert literal(fname, pattern) == float(exact), (fname, pattern)
