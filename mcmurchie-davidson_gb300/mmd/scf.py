@@ -458,6 +458,36 @@ class SCF(object):
         self.buildFock()
         self.orthoFock()
 
+    def updateDIIS(self, F, P):
+        """One DIIS step on host arrays, as the reference's helper (mmd/scf.py:146-180):
+        the error X (FPS - SPF) X of (F, P) and the *current* ``self.F`` join the
+        8-deep histories ``self.errorSet`` / ``self.fockSet`` (created empty when
+        absent), and the returned complex N x N matrix is the history combination
+        whose weights minimise the combined error under sum(w) = 1.  The SCF loop
+        itself runs the device version of the same step."""
+        if getattr(self, "fockSet", None) is None:
+            self.fockSet = []
+        if getattr(self, "errorSet", None) is None:
+            self.errorSet = []
+        FPS = np.asarray(F) @ np.asarray(P) @ np.asarray(self.S)
+        X = np.asarray(self.X)
+        self.fockSet.append(self.F)
+        self.errorSet.append(X @ (FPS - self.adj(FPS)) @ X)
+        while len(self.fockSet) > 8:
+            self.fockSet.pop(0)
+            self.errorSet.pop(0)
+        n = len(self.fockSet)
+        E = np.stack(self.errorSet)
+        B = np.full((n + 1, n + 1), -1.0)
+        B[:n, :n] = np.einsum("iab,jab->ij", E.conj(), E).real  # Re tr(e_i^H e_j)
+        B[n, n] = 0.0
+        rhs = np.zeros(n + 1)
+        rhs[n] = -1.0
+        w = np.linalg.solve(B, rhs)
+        assert np.isclose(w[:n].sum(), 1.0)
+        return np.tensordot(w[:n], np.stack(self.fockSet), axes=1).astype(complex).reshape(
+            self.nbasis, self.nbasis)
+
 
 class _RHFState:
     """One RHF run on the device; ``iterate()`` is one pass of mmd/scf.py:30-60."""

@@ -492,3 +492,45 @@ def test_device_constants_are_correctly_rounded():
     ]
     for fname, pattern, exact in cases:
         assert literal(fname, pattern) == float(exact), (fname, pattern)
+
+
+def test_update_diis_host_helper_matches_the_reference_steps():
+    """SCF.updateDIIS (host arrays, the reference's public helper mmd/scf.py:146-180)
+    against a loop restatement: the current self.F joins the history (not the F
+    argument), the error is X (FPS - SPF) X, B_ij = Re tr(e_i^H e_j), 8-deep window,
+    complex result."""
+    import types
+    from mmd.scf import SCF
+    rng = np.random.default_rng(12)
+    n = 5
+    A = rng.standard_normal((n, n))
+    S = A @ A.T + n * np.eye(n)
+    w, U = np.linalg.eigh(S)
+    X = (U / np.sqrt(w)) @ U.T
+    mol = types.SimpleNamespace(S=S, X=X, nbasis=n, adj=lambda x: np.conjugate(x).T)
+    rf, re_ = [], []
+    for k in range(11):
+        Fc = rng.standard_normal((n, n)); Fc = Fc + Fc.T        # self.F
+        Fa = rng.standard_normal((n, n)); Fa = Fa + Fa.T        # the F argument
+        P = rng.standard_normal((n, n)); P = P + P.T
+        mol.F = Fc.astype(complex)
+        got = SCF.updateDIIS(mol, Fa, P)
+        FPS = Fa @ P @ S
+        rf.append(Fc)
+        re_.append(X @ (FPS - FPS.T) @ X)
+        if len(rf) > 8:
+            del rf[0], re_[0]
+        m = len(rf)
+        B = np.zeros((m + 1, m + 1))
+        B[-1, :] = B[:, -1] = -1.0
+        B[-1, -1] = 0.0
+        for i in range(m):
+            for j in range(i + 1):
+                B[i, j] = B[j, i] = np.trace(re_[i].T @ re_[j])
+        r = np.zeros(m + 1)
+        r[-1] = -1.0
+        wts = np.linalg.solve(B, r)
+        ref = sum(wts[i] * rf[i] for i in range(m))
+        assert got.dtype == complex and got.shape == (n, n)
+        assert len(mol.fockSet) == m == len(mol.errorSet)
+        assert np.abs(got - ref).max() < 1e-10 * max(1.0, np.abs(ref).max())
