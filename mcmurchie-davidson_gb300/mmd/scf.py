@@ -356,6 +356,7 @@ class SCF(object):
         K = torch.empty_like(P)
         ctx.jk_dense(self._TwoE_dev, P.contiguous(), J, K)
         self.fock_builds += 1
+        self._last_jk = (J, K)  # the reference leaves the last J and K on the molecule
         return self._dev["Core"] + 2.0 * J - K
 
     def _diis(self, F, P, S, X, fockSet, errorSet):
@@ -521,6 +522,7 @@ class _RHFState:
         self.fockSet, self.errorSet, self.err_hist = [], [], []
         self.energy = None
         self.FO = None
+        self.F_old = None
         self.step = 0
         self.last_dP = None
 
@@ -531,6 +533,7 @@ class _RHFState:
         X, S, Core = self.X, self.S, self.Core
         if self.step > 0:
             F_old = self.F
+            self.F_old = F_old
             energy_old = self.energy
             if mol.direct:
                 self.last_dP = (self.P, self.P_old)
@@ -596,7 +599,9 @@ class _RHFState:
         reference's types: P, P_old, F, FO, C and CO complex128 (mmd/scf.py:15,24 start
         them complex; the imaginary parts are zero for RHF), the orbital energies MO
         real.  The energy stays a real float64 (the reference's carries a zero
-        imaginary part)."""
+        imaginary part).  Like the reference's loop, the molecule also keeps F_old
+        (the Fock matrix before the last build) and, after a conventional run, the
+        last build's J and K (complex128)."""
         mol = self.mol
         if self.E is None:  # the last iteration solved for the occupied orbitals only
             self._dense_solve()
@@ -610,3 +615,8 @@ class _RHFState:
         mol.MO = self.E.cpu().numpy()
         mol.energy = np.float64(self.energy)
         mol.el_energy = mol.energy - mol.nuc_energy
+        if self.F_old is not None:
+            mol.F_old = cplx(self.F_old)
+        jk = getattr(mol, "_last_jk", None)
+        if not mol.direct and jk is not None:
+            mol.J, mol.K = cplx(jk[0]), cplx(jk[1])

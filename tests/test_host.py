@@ -534,3 +534,30 @@ def test_update_diis_host_helper_matches_the_reference_steps():
         assert got.dtype == complex and got.shape == (n, n)
         assert len(mol.fockSet) == m == len(mol.errorSet)
         assert np.abs(got - ref).max() < 1e-10 * max(1.0, np.abs(ref).max())
+
+
+def test_rhf_results_keep_the_reference_attributes():
+    """_RHFState.finish hands back the reference's attributes as complex host arrays,
+    including F_old (the Fock matrix before the last build, mmd/scf.py:32) and, after
+    a conventional run, the last build's J and K (mmd/scf.py:97-98); run on CPU tensors."""
+    import types
+    import torch
+    from mmd.scf import _RHFState
+    n = 4
+    gen = torch.Generator().manual_seed(3)
+    t = lambda: torch.randn(n, n, dtype=torch.float64, generator=gen)
+    for direct in (False, True):
+        mol = types.SimpleNamespace(nuc_energy=1.0, direct=direct, _last_jk=(t(), t()))
+        st = _RHFState.__new__(_RHFState)
+        st.mol, st.E, st.energy = mol, torch.arange(n, dtype=torch.float64), -5.0
+        st.P, st.P_old, st.F, st.FO, st.C, st.CO, st.F_old = (t() for _ in range(7))
+        _RHFState.finish(st)
+        for name in ("P", "P_old", "F", "FO", "C", "CO", "F_old"):
+            assert getattr(mol, name).dtype == np.complex128, name
+        assert np.array_equal(mol.F_old.real, st.F_old.numpy())
+        assert mol.el_energy == -6.0 and mol.MO.dtype == np.float64
+        if direct:
+            assert not hasattr(mol, "J")
+        else:
+            assert np.array_equal(mol.J.real, mol._last_jk[0].numpy())
+            assert np.array_equal(mol.K.real, mol._last_jk[1].numpy())
