@@ -3,6 +3,7 @@
 ``S(a, b)``, ``T(a, b)``, ``V(a, b, C)`` and ``Mu(a, b, C, direction)`` keep the
 signatures of cython/onee.pyx:14-69; they evaluate the pair on the GPU
 (``mmdg_one_electron``).  ``Molecule`` computes whole matrices in one launch.
+``RxDel`` is importable but raises (no consumer of the angular-momentum integrals).
 ``_boys(n, T)`` is the Boys-function test hook (cython/onee.pyx:195-196), served
 by the GPU Boys kernel for integer orders 0..8 (the orders the ERI path uses).
 """
@@ -57,6 +58,13 @@ def Mu(a, b, C, direction):
     """Dipole integral about origin C (onee.pyx:27-36)."""
     k = {"x": 0, "y": 1, "z": 2}[direction.lower()]
     return float(_pair_matrices(a, b, origin=C)[3][k, 0, 1])
+
+
+def RxDel(a, b, C, direction):
+    """Angular-momentum integral (onee.pyx:36-46): importable under the reference's
+    name, but not evaluated here -- nothing in the reference reads ``Molecule.L``, and
+    it is no part of the two-electron path this package serves."""
+    raise NotImplementedError("RxDel: the angular-momentum integrals are not implemented on the GPU path")
 
 
 def _boys(n, T):
