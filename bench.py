@@ -882,7 +882,8 @@ def reference_arm(args):
             "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded cluster geometry)", "config": dict(WORKLOAD),
             "cpu_baseline": {"value": v, "unit": "Fock builds/s", "cores": cb["cores"], "kind": cb["kind"],
-                             "sample": cb["sample"], "anchor": cb.get("anchor")},
+                             "sample": cb["sample"], "t_build_1core_s": cb["t_build_1core_s"],
+                             "quartets_per_s_1core": cb["quartets_per_s_1core"], "anchor": cb.get("anchor")},
             "e2e": {"value": v, "unit": "Fock builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -70,5 +70,6 @@ def test_reference_arm_prints_the_contract_line():
     assert line["value"] > 0 and line["higher_is_better"] is True
     assert line["config"]["workload"] == bench.WORKLOAD["workload"]
     assert line["cpu_baseline"]["kind"] == "reference" and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["t_build_1core_s"] > 0 and line["cpu_baseline"]["quartets_per_s_1core"] > 0
     assert line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
