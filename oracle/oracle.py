@@ -233,13 +233,14 @@ def eri_unique(bfs, ij_lo, ij_hi):
     return out[:n]
 
 
-def eri_shell(bfs, fa, fb, fc, fd):
+def eri_shell(bfs, fa, fb, fc, fd, pack=None):
     """All component ERIs of four shells given as function-index lists (each list one
     Cartesian shell: same origin and exponents); array [len(fa), len(fb), len(fc), len(fd)],
-    equal bit for bit to ERI() per function quartet."""
+    equal bit for bit to ERI() per function quartet.  ``pack`` (a _Pack of ``bfs``)
+    saves re-packing the basis on every call."""
     arrs = [np.ascontiguousarray(x, dtype=np.int64) for x in (fa, fb, fc, fd)]
     out = np.zeros(tuple(len(a) for a in arrs))
-    pk = _Pack(bfs)
+    pk = pack if pack is not None else _Pack(bfs)
     lib().oracle_eri_shell(pk.ptr, arrs[0].ctypes.data, len(arrs[0]), arrs[1].ctypes.data, len(arrs[1]),
                            arrs[2].ctypes.data, len(arrs[2]), arrs[3].ctypes.data, len(arrs[3]), out.ctypes.data)
     return out
@@ -279,7 +280,26 @@ def _w_unique(args):
 
 
 def _w_shell(args):
-    return [eri_shell(_WB, *q) for q in args]
+    pk = _Pack(_WB)
+    return [eri_shell(_WB, *q, pack=pk) for q in args]
+
+
+def _w_shell_unique(args):
+    """Unique-ERI positions (doERIs loop order) and values of a chunk of shell
+    quartets: every component of each block, mapped to its canonical (ij|kl)."""
+    quartets, shells = args
+    pk = _Pack(_WB)
+    pos, val = [], []
+    for q in quartets:
+        fl = [shells[s] for s in q]
+        blk = eri_shell(_WB, *fl, pack=pk)
+        i, j, k, l = (x.ravel() for x in np.meshgrid(*[np.asarray(f, dtype=np.int64) for f in fl], indexing="ij"))
+        ij = np.where(i >= j, i * (i + 1) // 2 + j, j * (j + 1) // 2 + i)
+        kl = np.where(k >= l, k * (k + 1) // 2 + l, l * (l + 1) // 2 + k)
+        hi, lo = np.maximum(ij, kl), np.minimum(ij, kl)
+        pos.append(hi * (hi + 1) // 2 + lo)
+        val.append(blk.ravel())
+    return np.concatenate(pos), np.concatenate(val)
 
 
 def _ij_ranges(N, parts):
@@ -315,6 +335,31 @@ def parallel_eri_unique(bfs, nproc=None):
     with pool:
         parts = pool.map(_w_unique, _ij_ranges(N, 4 * n))
     return np.concatenate(parts)
+
+
+def parallel_eri_unique_shells(bfs, shells, nproc=None):
+    """The vector of parallel_eri_unique (every unique ERI in doERIs loop order) from
+    shell blocks: ``shells`` lists each shell's function indices (contiguous, in
+    function order); every shell quartet with the larger shell pair first is
+    evaluated once by eri_shell (memoised E and R, equal bit for bit to ERI for the
+    block's own function order) and each component lands at its canonical position.
+    A canonical quartet whose block holds it in another function order (the same
+    integral by permutational symmetry) may differ from ERI in the last bits."""
+    N = len(bfs)
+    shells = [[int(f) for f in sh] for sh in shells]
+    pairs = [(a, b) for a in range(len(shells)) for b in range(a + 1)]
+    quartets = [pairs[p] + pairs[r] for p in range(len(pairs)) for r in range(p + 1)]
+    pool, n = _pool(bfs, nproc)
+    chunks = [(quartets[k::8 * n], shells) for k in range(8 * n)]
+    with pool:
+        res = pool.map(_w_shell_unique, chunks)
+    npair = N * (N + 1) // 2
+    out = np.full(npair * (npair + 1) // 2, np.nan)
+    for pos, val in res:
+        out[pos] = val
+    if np.isnan(out).any():
+        raise ValueError("parallel_eri_unique_shells: the shells do not cover every function")
+    return out
 
 
 def parallel_eri_shells(bfs, quartets, nproc=None):

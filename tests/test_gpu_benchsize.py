@@ -12,7 +12,8 @@ seeded water clusters of the workload (6-31G**, Cartesian d).
   random shell order; every component ERI (mmdg_eri_quartets) against the oracle's
   ERI (twoe.pyx:36-50), absolute 1e-12 and relative 1e-9 where |ERI| > 1e-6.
 
-The oracle runs in a pool of processes (spawned) over the host's cores.
+The oracle runs in a pool of processes (spawned) over the host's cores, one shell
+quartet at a time with E and R memoised (the per-function form took 24x longer).
 """
 import os
 
@@ -104,14 +105,17 @@ def _densities(mol):
 def test_full_eri_tensor_and_formPT_of_water_clusters_vs_oracle(n):
     import oracle as O
     from mmd.integrals.fock import formPT
+    from mmd.integrals.shells import shells_from_bfs
     from mmd.integrals.twoe import doERIs
     mol = _cluster(n)
     N = mol.nbasis
     ob = oracle_bfs(mol)
-    # ERI tensor: every unique quartet
+    # ERI tensor: every unique quartet (the oracle evaluates each shell quartet once,
+    # memoised; pinned to its per-function ERI in the CPU suite)
     T = doERIs(N, np.zeros((N, N, N, N)), mol.bfs)
     i, j, k, l = O.unique_index(N)
-    ref = O.parallel_eri_unique(ob)
+    shells = [[int(f) for f in row if f >= 0] for row in shells_from_bfs(mol.bfs).func]
+    ref = O.parallel_eri_unique_shells(ob, shells)
     err = np.abs(T[i, j, k, l] - ref)
     assert err.max() < 1e-12, (n, err.max())
     del T

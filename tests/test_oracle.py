@@ -191,6 +191,26 @@ def test_ranged_unique_eris_equal_doERIs(golden):
         k0 += 1
 
 
+def test_shell_blocked_unique_eris_equal_the_per_function_ones(golden):
+    """parallel_eri_unique_shells (every shell quartet once, components scattered to
+    their canonical positions) against the per-function unique ERIs of doERIs order:
+    water/6-31G** with its d shell, equal to 1e-15 (blocks that hold a canonical
+    quartet in another function order differ in the last bits only); a shell list
+    missing a function is refused."""
+    from mmd.integrals.shells import shells_from_bfs
+    from mmd.molecule import Molecule
+    d = golden("mol_water_631gss.npz")
+    bfs = _raw_bfs(d)
+    shells = [[int(f) for f in row if f >= 0] for row in
+              shells_from_bfs(Molecule(str(d["geometry"]), str(d["basis"])).bfs).func]
+    ref = O.parallel_eri_unique(bfs, nproc=2)
+    got = O.parallel_eri_unique_shells(bfs, shells, nproc=2)
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 1e-15
+    with pytest.raises(ValueError):
+        O.parallel_eri_unique_shells(bfs, shells[:-1], nproc=2)
+
+
 def test_partial_formPT_adds_up_to_formPT(golden):
     """formPT restricted to ij ranges, or to the shell quartets of each part of a
     shell-pair partition, adds up to the full formPT (the reference's records)."""
