@@ -27,6 +27,12 @@ def _fact2(k: int) -> float:
     return r
 
 
+# (shell, raw exponents, raw coefficients) -> (norm, normalised coefficients): every
+# function of an element's shell type shares them, so a molecule normalises each once
+_NORMALISED: dict = {}
+_NORMALISED_MAX = 4096
+
+
 class Basis:
     """Contracted Cartesian Gaussian function (cython/basis.pxi:6-121).
 
@@ -45,8 +51,16 @@ class Basis:
             raise ValueError("a basis function needs at least one primitive")
         self.exps = np.array(exps, dtype=np.float64)[: self.num_exps].copy()
         self.coefs = np.array(coefs, dtype=np.float64)[: self.num_exps].copy()
-        self.norm = np.zeros(self.num_exps)
-        self.normalize()
+        key = (self.shell.tobytes(), self.exps.tobytes(), self.coefs.tobytes())
+        done = _NORMALISED.get(key)
+        if done is None:
+            self.norm = np.zeros(self.num_exps)
+            self.normalize()
+            if len(_NORMALISED) < _NORMALISED_MAX:
+                _NORMALISED[key] = (self.norm.copy(), self.coefs.copy())
+        else:  # the same arithmetic on the same inputs: bit-identical results
+            self.norm = done[0].copy()
+            self.coefs = done[1].copy()
 
     def normalize(self):
         """Primitive then contracted normalisation (basis.pxi:87-120)."""

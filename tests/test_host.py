@@ -561,3 +561,22 @@ def test_rhf_results_keep_the_reference_attributes():
         else:
             assert np.array_equal(mol.J.real, mol._last_jk[0].numpy())
             assert np.array_equal(mol.K.real, mol._last_jk[1].numpy())
+
+
+def test_memoised_basis_normalisation_is_bit_identical():
+    """Basis functions with the same shell, exponents and coefficients reuse one
+    normalisation: bit-identical to normalising afresh, and each function owns copies."""
+    from mmd.integrals import twoe
+    ex, co = [5.0331513, 1.1695961, 0.3803890], [-0.09996723, 0.39951283, 0.70011547]
+    twoe._NORMALISED.clear()
+    a = twoe.Basis([0.0, 0.0, 0.0], (1, 1, 0), 3, ex, co)   # computed
+    b = twoe.Basis([1.0, 2.0, 3.0], (1, 1, 0), 3, ex, co)   # from the memo
+    twoe._NORMALISED.clear()
+    c = twoe.Basis([1.0, 2.0, 3.0], (1, 1, 0), 3, ex, co)   # computed again
+    for x in (a, b):
+        assert np.array_equal(x.norm, c.norm) and np.array_equal(x.coefs, c.coefs)
+    b.coefs[0] = 0.0
+    d = twoe.Basis([0.0, 0.0, 0.0], (1, 1, 0), 3, ex, co)
+    assert np.array_equal(d.coefs, c.coefs) and not np.shares_memory(d.coefs, c.coefs)
+    e = twoe.Basis([0.0, 0.0, 0.0], (2, 0, 0), 3, ex, co)   # another shell: its own entry
+    assert not np.array_equal(e.norm, c.norm)
